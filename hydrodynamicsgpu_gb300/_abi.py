@@ -1,0 +1,115 @@
+"""ctypes mirror of include/hgpu/hgpu.h (types, enums and name registries).
+
+The name registries are the string keys the reference reads from its Lua config:
+solver names (src/HydroGPUApp.cpp:90-118), integrator names
+(src/Solver/Solver.cpp:178-204), slope limiter names (res/SlopeLimiter.cl:5-68,
+read from the key ``slopeLimiter`` at src/Solver/Solver.cpp:285-287) and boundary
+method names (src/Equation/Euler.cpp:30-34, "NONE" at src/HydroGPUApp.cpp:505-507).
+"""
+import ctypes
+
+HGPU_OK = 0
+STATUS_NAMES = {
+    0: "HGPU_OK", 1: "HGPU_ERR_CONFIG", 2: "HGPU_ERR_CUDA", 3: "HGPU_ERR_NONFINITE",
+    4: "HGPU_ERR_TIMEOUT", 5: "HGPU_ERR_OOB", 6: "HGPU_ERR_ARG", 7: "HGPU_ERR_UNSUPPORTED",
+    8: "HGPU_ERR_NOMEM",
+}
+
+SOLVERS = {"EulerRoe": 0, "EulerHLLC": 1}
+BOUNDARIES = {"NONE": -1, "PERIODIC": 0, "MIRROR": 1, "FREEFLOW": 2}
+LIMITERS = ["DonorCell", "LaxWendroff", "BeamWarming", "Fromm", "CHARM", "HCUS", "HQUICK",
+            "Koren", "MinMod", "Oshker", "Ospre", "Smart", "Sweby", "UMIST", "VanAlbada1",
+            "VanAlbada2", "VanLeer", "MonotizedCentral", "Superbee", "BarthJespersen"]
+INTEGRATORS = ["ForwardEuler", "RungeKutta2", "RungeKutta2Heun", "RungeKutta2Ralston", "RungeKutta3",
+               "RungeKutta4", "RungeKutta4_3_8thsRule", "RungeKutta2TVD", "RungeKutta2NonTVD",
+               "RungeKutta3TVD", "RungeKutta4TVD", "RungeKutta4NonTVD"]
+INTEGRATOR_ORDER = [1, 2, 2, 2, 3, 4, 4, 2, 2, 3, 4, 4]
+FP64, FP32 = 0, 1
+COMPAT_REF, COMPAT_SEAM = 0, 1
+
+
+class HgpuConfig(ctypes.Structure):
+    _fields_ = [
+        ("solver", ctypes.c_int),
+        ("dim", ctypes.c_int),
+        ("size", ctypes.c_int * 3),
+        ("xmin", ctypes.c_double * 3),
+        ("xmax", ctypes.c_double * 3),
+        ("gamma", ctypes.c_double),
+        ("cfl", ctypes.c_float),
+        ("use_fixed_dt", ctypes.c_int),
+        ("fixed_dt", ctypes.c_double),
+        ("boundary", (ctypes.c_int * 2) * 3),
+        ("limiter", ctypes.c_int),
+        ("integrator", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("compat", ctypes.c_int),
+        ("reserved", ctypes.c_int * 8),
+    ]
+
+
+def _index(name, table, what):
+    if isinstance(name, int):
+        return name
+    if isinstance(table, dict):
+        if name not in table:
+            raise ValueError("unknown %s %r" % (what, name))
+        return table[name]
+    if name not in table:
+        raise ValueError("unknown %s %r" % (what, name))
+    return table.index(name)
+
+
+def make_config(solver="EulerRoe", size=(256, 256), xmin=(-.5, -.5, -.5), xmax=(.5, .5, .5), gamma=1.4,
+                cfl=.5, use_fixed_dt=False, fixed_dt=.001, boundary="FREEFLOW", limiter="Superbee",
+                integrator="ForwardEuler", precision=FP64, compat=COMPAT_REF, dim=0):
+    """Build an HgpuConfig from the reference's config key values.
+
+    ``size`` lists cells per axis including the 2 ghost layers per side (the
+    reference's ``size`` key); missing axes are 1.  ``boundary`` is one name for
+    every side, or a sequence of per-axis ``{"min": name, "max": name}`` dicts /
+    ``(min, max)`` pairs (the reference's ``boundaryMethods`` table)."""
+    cfg = HgpuConfig()
+    cfg.solver = _index(solver, SOLVERS, "solver")
+    cfg.dim = dim
+    size = list(size) + [1] * (3 - len(size))
+    xmin = list(xmin) + [-.5] * (3 - len(xmin))
+    xmax = list(xmax) + [.5] * (3 - len(xmax))
+    for i in range(3):
+        cfg.size[i] = int(size[i])
+        cfg.xmin[i] = float(xmin[i])
+        cfg.xmax[i] = float(xmax[i])
+    cfg.gamma = float(gamma)
+    cfg.cfl = float(cfl)
+    cfg.use_fixed_dt = int(bool(use_fixed_dt))
+    cfg.fixed_dt = float(fixed_dt)
+    if isinstance(boundary, (str, int)):
+        boundary = [(boundary, boundary)] * 3
+    for i in range(3):
+        b = boundary[i] if i < len(boundary) else ("NONE", "NONE")
+        if isinstance(b, dict):
+            b = (b.get("min", "NONE"), b.get("max", "NONE"))
+        cfg.boundary[i][0] = _index(b[0], BOUNDARIES, "boundary method")
+        cfg.boundary[i][1] = _index(b[1], BOUNDARIES, "boundary method")
+    cfg.limiter = _index(limiter, LIMITERS, "slope limiter")
+    cfg.integrator = _index(integrator, INTEGRATORS, "integrator")
+    cfg.precision = int(precision)
+    cfg.compat = int(compat)
+    return cfg
+
+
+def config_dim(cfg):
+    if cfg.dim:
+        return cfg.dim
+    for d in (3, 2, 1):
+        if cfg.size[d - 1] > 1:
+            return d
+    return 0
+
+
+def config_volume(cfg):
+    return int(cfg.size[0]) * int(cfg.size[1]) * int(cfg.size[2])
+
+
+def config_count(cfg):
+    return config_volume(cfg) * (config_dim(cfg) + 2)

@@ -1,0 +1,208 @@
+/*
+ * hgpu.h -- C ABI of the GB300-native finite-volume Euler update.
+ *
+ * This is the drop-in boundary for HydroGPU's OpenCL solver path
+ * (KennethYeah/HydrodynamicsGPU).  The reference has no C ABI: its host app
+ * drives C++ classes (HydroGPUApp -> ISolver/Solver -> Integrator -> OpenCL
+ * kernels).  Each entry point below replaces one reference interface; the
+ * replaced interface is cited beside it as file:line of the reference project.
+ *
+ * Conventions
+ *  - Plain C types only; no exceptions cross this boundary.  Every function
+ *    returns an hgpu_status (0 = HGPU_OK).
+ *  - State arrays use the reference layout: array-of-structures, ghost cells
+ *    included, element (state j, cell x,y,z) at
+ *        j + N * (x + SIZE_X * (y + SIZE_Y * z))
+ *    (res/include/HydroGPU/Shared/Common.h:59-60, res/Roe.cl:106-108), with
+ *    N = dim + 2 conserved states: density, momentum x..(dim), total energy
+ *    (src/Equation/Euler.cpp:36-40).
+ *  - Element type is double for HGPU_FP64 solvers and float for HGPU_FP32.
+ *  - The library owns all device memory.  A handle is used by one host thread
+ *    at a time; different handles are independent.
+ */
+#ifndef HGPU_HGPU_H
+#define HGPU_HGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HGPU_ABI_VERSION 1
+
+/* ---- status codes (replace the reference's C++ exceptions:
+ *      src/Solver/Solver.cpp:150,201; src/HydroGPUApp.cpp:347,509) ---- */
+typedef enum hgpu_status {
+    HGPU_OK = 0,
+    HGPU_ERR_CONFIG = 1,      /* invalid configuration value                  */
+    HGPU_ERR_CUDA = 2,        /* a CUDA runtime/driver call failed            */
+    HGPU_ERR_NONFINITE = 3,   /* NaN/Inf in the CFL reduction or the state    */
+    HGPU_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up           */
+    HGPU_ERR_OOB = 5,         /* a size/offset argument is out of range       */
+    HGPU_ERR_ARG = 6,         /* NULL handle/pointer or wrong element count   */
+    HGPU_ERR_UNSUPPORTED = 7, /* combination not provided by this build       */
+    HGPU_ERR_NOMEM = 8        /* device allocation failed                     */
+} hgpu_status;
+
+/* ---- solver family (src/HydroGPUApp.cpp:90-118 solver registry) ---- */
+enum {
+    HGPU_SOLVER_ROE = 0,   /* "EulerRoe"  (src/Solver/EulerRoe.cpp)  */
+    HGPU_SOLVER_HLLC = 1   /* "EulerHLLC" (src/Solver/EulerHLLC.cpp) */
+};
+
+/* ---- boundary methods (include/HydroGPU/Boundary/Boundary.h:8-14; the
+ *      "MIRROR" method reflects the normal momentum, src/Equation/Euler.cpp:63-75) ---- */
+enum {
+    HGPU_BOUNDARY_NONE = -1,
+    HGPU_BOUNDARY_PERIODIC = 0,
+    HGPU_BOUNDARY_MIRROR = 1,
+    HGPU_BOUNDARY_FREEFLOW = 2
+};
+
+/* ---- slope limiters, in the order of res/SlopeLimiter.cl:5-68 ---- */
+enum {
+    HGPU_LIMITER_DONORCELL = 0,
+    HGPU_LIMITER_LAXWENDROFF,
+    HGPU_LIMITER_BEAMWARMING,
+    HGPU_LIMITER_FROMM,
+    HGPU_LIMITER_CHARM,
+    HGPU_LIMITER_HCUS,
+    HGPU_LIMITER_HQUICK,
+    HGPU_LIMITER_KOREN,
+    HGPU_LIMITER_MINMOD,
+    HGPU_LIMITER_OSHKER,
+    HGPU_LIMITER_OSPRE,
+    HGPU_LIMITER_SMART,
+    HGPU_LIMITER_SWEBY,
+    HGPU_LIMITER_UMIST,
+    HGPU_LIMITER_VANALBADA1,
+    HGPU_LIMITER_VANALBADA2,
+    HGPU_LIMITER_VANLEER,
+    HGPU_LIMITER_MONOTIZEDCENTRAL,
+    HGPU_LIMITER_SUPERBEE,
+    HGPU_LIMITER_BARTHJESPERSEN,
+    HGPU_NUM_LIMITERS
+};
+
+/* ---- integrators (src/Solver/Solver.cpp:178-204 registry;
+ *      tableaus include/HydroGPU/Integrator/RungeKutta.h:129-294).
+ *      BackwardEulerConjugateGradient is not provided: the reference's
+ *      version throws unconditionally (src/Integrator/BackwardEulerConjugateGradient.cpp:80). ---- */
+enum {
+    HGPU_INTEGRATOR_FORWARD_EULER = 0,
+    HGPU_INTEGRATOR_RK2,            /* RungeKutta2 (midpoint)   */
+    HGPU_INTEGRATOR_RK2_HEUN,
+    HGPU_INTEGRATOR_RK2_RALSTON,
+    HGPU_INTEGRATOR_RK3,
+    HGPU_INTEGRATOR_RK4,
+    HGPU_INTEGRATOR_RK4_38,         /* RungeKutta4_3_8thsRule   */
+    HGPU_INTEGRATOR_RK2_TVD,
+    HGPU_INTEGRATOR_RK2_NONTVD,
+    HGPU_INTEGRATOR_RK3_TVD,
+    HGPU_INTEGRATOR_RK4_TVD,
+    HGPU_INTEGRATOR_RK4_NONTVD,
+    HGPU_NUM_INTEGRATORS
+};
+
+enum { HGPU_FP64 = 0, HGPU_FP32 = 1 };
+
+/* Numerical compatibility.
+ *  HGPU_COMPAT_REF : reproduce the reference step exactly, including its
+ *                    6-significant-digit DX literals, frozen per-step eigenbasis,
+ *                    never-written (zero) Delta-q-tilde at faces 1 and SIZE-1 and
+ *                    stale stage ghost cells.
+ *  HGPU_COMPAT_SEAM: same scheme, but eigenbasis/Delta-q-tilde also on faces 1 and
+ *                    SIZE-1 and a ghost refresh of every stage state, so periodic
+ *                    domains conserve totals to round-off. */
+enum { HGPU_COMPAT_REF = 0, HGPU_COMPAT_SEAM = 1 };
+
+/* Headless equivalent of the HydroGPUApp config fields the solver path reads
+ * (include/HydroGPU/HydroGPUApp.h:72-94; src/HydroGPUApp.cpp:164-208;
+ *  src/Solver/Solver.cpp:285-307). */
+typedef struct hgpu_config {
+    int solver;            /* HGPU_SOLVER_*                                              */
+    int dim;               /* 1..3, or 0 = last axis with size > 1 (HydroGPUApp.cpp:214-221) */
+    int size[3];           /* cells per axis INCLUDING 2 ghost layers per side; 1 = unused */
+    double xmin[3];        /* domain spans all SIZE cells; dx = (xmax-xmin)/size          */
+    double xmax[3];
+    double gamma;          /* defs.idealGas_heatCapacityRatio (Lua number)               */
+    float cfl;             /* a C float, as in HydroGPUApp.h:84                           */
+    int use_fixed_dt;
+    double fixed_dt;
+    int boundary[3][2];    /* [axis][min,max] of HGPU_BOUNDARY_*                          */
+    int limiter;           /* HGPU_LIMITER_* ("slopeLimiter" key, Solver.cpp:285-287)     */
+    int integrator;        /* HGPU_INTEGRATOR_* ("integratorName" key)                    */
+    int precision;         /* HGPU_FP64 / HGPU_FP32                                       */
+    int compat;            /* HGPU_COMPAT_*                                               */
+    int reserved[8];       /* zero                                                        */
+} hgpu_config;
+
+typedef struct hgpu_solver hgpu_solver;  /* opaque handle */
+
+/* Fill *cfg with the reference's defaults (HydroGPUApp.cpp:60-126 constructor:
+ * cfl .5, fixedDT .001, xmin -.5, xmax .5; Solver.cpp:285 Superbee;
+ * Solver.cpp:196 ForwardEuler) for a 2D 256x256 EulerRoe run. */
+int hgpu_config_default(hgpu_config* cfg);
+
+/* Human-readable name of a status code. */
+const char* hgpu_status_string(int status);
+
+/* Validate cfg and create a solver: replaces Solver::init (src/Solver/Solver.cpp:48-205),
+ * i.e. NDRange setup, program build, initBuffers/initKernels and integrator selection.
+ * Allocates every device buffer the step needs; later calls allocate nothing. */
+int hgpu_create(const hgpu_config* cfg, hgpu_solver** out);
+
+/* Free the handle and all device memory it owns. */
+int hgpu_destroy(hgpu_solver* s);
+
+/* Number of cells V = size[0]*size[1]*size[2] and states N of a solver. */
+int hgpu_get_shape(const hgpu_solver* s, int* dim, int* num_states, size_t* volume);
+
+/* Upload a full state (ghosts included, AoS): replaces Solver::resetState's
+ * Converter::toGPU (src/Solver/Solver.cpp:333-337, SelfGravitation.cpp:89-97 with a
+ * zero potential).  count = V*N elements of the solver's precision. */
+int hgpu_set_state(hgpu_solver* s, const void* host_state, size_t count);
+
+/* Download the full state: replaces Converter::fromGPU (Solver.cpp:339-342). */
+int hgpu_get_state(hgpu_solver* s, void* host_state, size_t count);
+
+/* Advance nsteps time steps: each is Solver::update (src/Solver/Solver.cpp:521-546)
+ * = boundary(); initStep(); dt = useFixedDT ? fixedDT : calcTimestep(); step(dt)
+ * with EulerRoe::step / EulerHLL::step including SelfGravitation::applyPotential
+ * (src/Solver/EulerRoe.cpp:31-34, EulerHLL.cpp:25-28).  dt stays on the device;
+ * the call returns after the last step's work is queued and, if last_dt is
+ * non-NULL, after it finished, with that step's dt.  */
+int hgpu_update(hgpu_solver* s, int nsteps, double* last_dt);
+
+/* dt of the most recent step (blocks on the solver's stream). */
+int hgpu_last_dt(hgpu_solver* s, double* dt);
+
+/* Wait for queued work; returns HGPU_ERR_NONFINITE if a step saw NaN in the
+ * CFL reduction (health word), HGPU_ERR_CUDA on a CUDA error. */
+int hgpu_synchronize(hgpu_solver* s);
+
+/* Read and clear the device-side health word (bit 0: non-finite dt seen;
+ * bit 1: HLLC interface with no flux branch taken). */
+int hgpu_health(hgpu_solver* s, uint32_t* flags);
+
+/* Device pointer of the current state buffer (for device-resident pipelines;
+ * the buffer is owned by the solver). */
+int hgpu_state_device_ptr(hgpu_solver* s, void** dptr);
+
+/* CUDA stream the solver launches on (a cudaStream_t). */
+int hgpu_stream(hgpu_solver* s, void** stream);
+
+/* Use CUDA-graph replay for hgpu_update (default on; off runs the same kernels
+ * as plain launches). */
+int hgpu_set_graphs(hgpu_solver* s, int enabled);
+
+/* Number of kernels one step launches (for launch accounting). */
+int hgpu_kernels_per_step(const hgpu_solver* s, int* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HGPU_HGPU_H */
