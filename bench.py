@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""Benchmark: 2D Euler Roe cell-updates/s on one GB300 (FP64), HydroGPU's KH workload.
+
+Workload (the 2D benchmark configuration): EulerRoe, FP64, 2048x2048 cells (ghosts
+included) on [-0.5,0.5]^2, periodic, gamma 1.4, minmod limiter, RK4, CFL 0.5,
+Kelvin-Helmholtz shear-layer IC (seeded synthetic noise).  A "step" is one full
+Solver::update (all four RK stages).  A cell-update is one interior cell advanced
+by one step.
+
+  python bench.py [--gpus N --steps K --warmup W]          # this repository (GB300 kernels)
+  python bench.py --impl reference [--steps K --warmup W]   # the reference's kernels on the host CPU
+
+`value` is device time (CUDA events on the solver's stream around K graph
+replays, inputs resident in HBM); `e2e` runs the same K steps through the C ABI
+with the state uploaded from and downloaded to page-locked host memory every step.
+With N > 1 (torchrun) every rank runs an independent replica on its own GPU
+(the workload does not shard across GPUs in the reference; "replicas only").
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "2D Euler Roe cell-updates/s (FP64, 1 GB300) plain vs batched; adjoint/fwd time"
+UNIT = "cell-updates/s"
+N_STATES = 4
+RECORD = 17              # doubles per face in the compact Roe eigenbasis record (2D)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def workload_config(hg_abi, size):
+    return hg_abi.make_config(solver="EulerRoe", size=(size, size), xmin=(-.5, -.5), xmax=(.5, .5), gamma=1.4,
+                              boundary="PERIODIC", limiter="MinMod", integrator="RungeKutta4", cfl=.5)
+
+
+def workload_name(size):
+    return "KH %dx%d EulerRoe FP64 RK4 minmod periodic CFL 0.5" % (size, size)
+
+
+# ---------------- clocks during the timed region ----------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------- CPU baselines (the reference's kernels on host cores) ----------------
+def cpu_sample(size, warm=1, steps=2):
+    """Bounded sample: the same scheme on a size x (size/4) strip of the KH workload."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    from hydrodynamicsgpu_gb300 import _abi, initconds as ic
+    ny = max(64, size // 4)
+    cfg = _abi.make_config(solver="EulerRoe", size=(size, ny), boundary="PERIODIC", limiter="MinMod",
+                           integrator="RungeKutta4", cfl=.5)
+    init = ic.kelvin_helmholtz(size=(size, ny), seed=0).reshape(-1)
+    kind = "reference"
+    try:
+        if not pyoracle.refcl_available(cfg):
+            pyoracle.build_refcl(quiet=True)
+        solver = pyoracle.Refcl(cfg)
+        cores = solver.max_threads()
+    except Exception:
+        kind = "port"
+        solver = pyoracle.Oracle(cfg)
+        cores = pyoracle.max_threads()
+    solver.set_state(init)
+    solver.update(warm)
+    t0 = time.perf_counter()
+    solver.update(steps)
+    dt = time.perf_counter() - t0
+    cells = (size - 4) * (ny - 4)
+    sample = "%d RK4 steps of the same scheme on a %dx%d strip of the KH workload (after %d warm-up)" % (
+        steps, size, ny, warm)
+    return {"value": cells * steps / dt, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}, dt
+
+
+def run_reference(args):
+    rank, local_rank, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    from hydrodynamicsgpu_gb300 import _abi, initconds as ic
+    size = args.size
+    ny = max(64, size // 8)
+    cfg = _abi.make_config(solver="EulerRoe", size=(size, ny), boundary="PERIODIC", limiter="MinMod",
+                           integrator="RungeKutta4", cfl=.5)
+    init = ic.kelvin_helmholtz(size=(size, ny), seed=0).reshape(-1)
+    kind = "reference"
+    try:
+        if not pyoracle.refcl_available(cfg):
+            pyoracle.build_refcl(quiet=True)
+        solver = pyoracle.Refcl(cfg)
+        cores = solver.max_threads()
+    except Exception:
+        kind = "port"
+        solver = pyoracle.Oracle(cfg)
+        cores = pyoracle.max_threads()
+    solver.set_state(init)
+    solver.update(args.warmup)
+    t0 = time.perf_counter()
+    solver.update(args.steps)
+    el = time.perf_counter() - t0
+    cells = (size - 4) * (ny - 4)
+    value = cells * args.steps / el
+    sample = ("each step: one RK4 step of the KH scheme on a %dx%d strip (same per-cell work as %dx%d), "
+              "the reference's OpenCL kernels compiled for the host CPU with OpenMP" % (size, ny, size, size))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded KH shear layer)",
+            "config": {"workload": workload_name(size), "sample_grid": [size, ny]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------- GB300 arm ----------------
+def algorithmic_bytes_per_cell(kind):
+    """Compulsory HBM bytes per interior cell for one launch of each kernel (2D, FP64).
+    One 'array' = N_STATES doubles per cell; the eigenbasis record is RECORD doubles per face."""
+    s = 8
+    face = 2  # faces per cell in 2D
+    table = {
+        "roe_flux": N_STATES * s + face * RECORD * s + face * N_STATES * s + face * N_STATES * s,
+        "roe_delta_q_tilde": N_STATES * s + face * (2 * N_STATES + 3) * s + face * N_STATES * s,
+        "roe_eigenbasis": N_STATES * s + face * RECORD * s,
+        "flux_divergence_combine": face * N_STATES * s + 4 * N_STATES * s,  # flux + ~4 state-sized arrays (RK4 mean)
+        "cfl_min_reduce": face * 2 * s,
+        "boundary": 0,
+        "finalize_dt": 0,
+    }
+    return table.get(kind, 0)
+
+
+def run_gb300(args):
+    rank, local_rank, world = dist_env()
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    import hydrodynamicsgpu_gb300 as hg
+    from hydrodynamicsgpu_gb300 import _abi, initconds as ic
+    if not os.path.exists(hg.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    hg.select_device(local_rank)
+
+    size = args.size
+    cfg = workload_config(_abi, size)
+    init = ic.kelvin_helmholtz(size=(size, size), seed=0).reshape(-1)
+    solver = hg.Solver(cfg)
+    solver.resetState(init)
+    interior = (size - 4) * (size - 4)
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    def max_over_ranks(x):
+        if not pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up (also captures the CUDA graph of one step)
+    solver.update(args.warmup, want_dt=False)
+    solver.synchronize()
+
+    # ---- timed region: K graph replays, CUDA events on the solver's stream ----
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    solver.synchronize()
+    ms = solver.timed_update(args.steps)
+    solver.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = max_over_ranks(ms)
+    kernels_per_step = solver.kernels_per_step()
+    ms_per_step = ms / args.steps
+    value = interior * args.steps * world / (ms * 1e-3)
+    health = solver.health()
+
+    # ---- per-kernel breakdown (plain launches, events around each launch) ----
+    prof = solver.profile(2)
+    dominant = max(prof.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_total) = dominant
+    dom_ms = dom_total / dom_launches
+    peak_gbs, peak_kind = measured_peaks()
+    bytes_per_launch = algorithmic_bytes_per_cell(dom_name) * interior
+    achieved_gbs = bytes_per_launch / (dom_ms * 1e-3) / 1e9
+    fp64_peak = hg.fp64_peak()
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": dom_ms,
+                "note": "FP64 issue rate, not HBM, bounds this kernel; see fp64"}
+    breakdown = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / sum(x[1] for x in prof.values())}
+                 for k, v in prof.items()}
+
+    # ---- e2e through the C ABI: H2D from pinned host, step, dt read, D2H to pinned host ----
+    e2e = None
+    if not args.no_e2e:
+        n = solver.count
+        host_in = hg.PinnedArray(n, np.float64)
+        host_out = hg.PinnedArray(n, np.float64)
+        host_in.array[:] = init
+        e2e_solver = hg.Solver(cfg)
+        e2e_solver.resetState(host_in.array)
+        e2e_solver.update(args.warmup)
+        e2e_solver.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_solver.resetState(host_in.array)          # hgpu_set_state (H2D)
+            e2e_solver.update(1)                           # hgpu_update, dt read back (8 B D2H)
+            e2e_solver.getState(host_out.array)            # hgpu_get_state (D2H)
+        el = time.perf_counter() - t0
+        barrier()
+        el = max_over_ranks(el)
+        e2e = {"value": interior * args.steps * world / el, "unit": UNIT,
+               "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8 + 8,
+               "ms_per_step": el / args.steps * 1e3}
+        e2e_solver.close()
+        host_in.free()
+        host_out.free()
+
+    # ---- CPU baseline (rank 0, N=1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, _ = cpu_sample(size)
+
+    fp64_per_cell_update = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded KH shear layer, random-phase noise)",
+        "config": {"workload": workload_name(size), "grid": [size, size], "solver": "EulerRoe",
+                   "integrator": "RungeKutta4", "limiter": "MinMod", "boundary": "periodic",
+                   "interior_cells": interior, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state 134 MB, eigenbasis 1.14 GB, fluxes 268 MB per step)"},
+        "roofline": roofline,
+        "fp64": {"fma_per_s_peak_measured": fp64_peak, "bound": "fp64 issue"},
+        "kernels": breakdown,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": kernels_per_step * args.steps,
+        "health_flags": health,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,244 @@
+"""hydrodynamicsgpu_gb300 -- GB300-native finite-volume Euler update (HydroGPU's solver path).
+
+The compute path is libhgpu.so: hand-written sm_103a CUDA kernels behind the C ABI
+of include/hgpu/hgpu.h.  This module is a thin ctypes mirror of that ABI plus a
+``Solver`` class with the reference's host interface (src/Solver/Solver.h:75-145):
+``init()``, ``resetState()``, ``update()``, ``save()``.  There is no CPU fallback:
+if libhgpu.so is missing or no GPU is present, the calls fail loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (COMPAT_REF, COMPAT_SEAM, FP32, FP64, HgpuConfig, INTEGRATORS, LIMITERS,  # noqa: F401
+                   SOLVERS, make_config)
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libhgpu.so")
+
+# every entry point of include/hgpu/hgpu.h: name -> (restype, argtypes)
+_P = ctypes.c_void_p
+_CFG = ctypes.POINTER(HgpuConfig)
+SIGNATURES = {
+    "hgpu_config_default": (ctypes.c_int, [_CFG]),
+    "hgpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "hgpu_last_error": (ctypes.c_char_p, []),
+    "hgpu_create": (ctypes.c_int, [_CFG, ctypes.POINTER(_P)]),
+    "hgpu_destroy": (ctypes.c_int, [_P]),
+    "hgpu_get_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_size_t)]),
+    "hgpu_set_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    "hgpu_get_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    "hgpu_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_last_dt": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_synchronize": (ctypes.c_int, [_P]),
+    "hgpu_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "hgpu_state_device_ptr": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "hgpu_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "hgpu_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
+    "hgpu_kernels_per_step": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "hgpu_select_device": (ctypes.c_int, [ctypes.c_int]),
+    "hgpu_timed_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "hgpu_profile_update": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "hgpu_fp64_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "hgpu_host_free": (ctypes.c_int, [_P]),
+}
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
+
+
+def select_device(device):
+    check(lib().hgpu_select_device(int(device)))
+
+
+def fp64_peak():
+    """Measured FP64 fma instructions per second of the current device."""
+    r = ctypes.c_double()
+    check(lib().hgpu_fp64_peak(ctypes.byref(r)))
+    return r.value
+
+class PinnedArray:
+    """A numpy view of a page-locked host buffer (hgpu_host_alloc)."""
+
+    def __init__(self, n, dtype):
+        dtype = np.dtype(dtype)
+        p = ctypes.c_void_p()
+        check(lib().hgpu_host_alloc(n * dtype.itemsize, ctypes.byref(p)))
+        self.ptr = p
+        buf = (ctypes.c_char * (n * dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=n)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            lib().hgpu_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+_lib = None
+
+
+class HgpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_abi.STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def lib():
+    """Load libhgpu.so (built in-tree by build()); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libhgpu.so not built: run __graft_entry__.build() or hydrodynamicsgpu_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != 0:
+        raise HgpuError(status, lib().hgpu_last_error().decode())
+
+
+class Solver:
+    """A GB300 Euler solver (EulerRoe or EulerHLLC) behind the C ABI.
+
+    Mirrors the reference's host interface: construct with a config (the
+    HydroGPUApp config fields), ``resetState(state)`` uploads an initial state
+    (AoS, ghosts included), ``update(n)`` runs Solver::update n times, ``getState()``
+    downloads it and ``save(prefix)`` writes one raw file per state channel."""
+
+    def __init__(self, cfg=None, **kw):
+        self.cfg = cfg if cfg is not None else make_config(**kw)
+        h = ctypes.c_void_p()
+        check(lib().hgpu_create(ctypes.byref(self.cfg), ctypes.byref(h)))
+        self.h = h
+        d, n, v = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+        check(lib().hgpu_get_shape(self.h, ctypes.byref(d), ctypes.byref(n), ctypes.byref(v)))
+        self.dim, self.num_states, self.volume = d.value, n.value, v.value
+        self.dtype = np.float32 if self.cfg.precision == FP32 else np.float64
+        self.frame = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def count(self):
+        return self.volume * self.num_states
+
+    def shape(self):
+        s = self.cfg.size
+        return (s[2], s[1], s[0], self.num_states)
+
+    def name(self):
+        return "EulerRoe" if self.cfg.solver == 0 else "EulerHLLC"
+
+    def resetState(self, state):
+        a = np.ascontiguousarray(state, dtype=self.dtype).reshape(-1)
+        if a.size != self.count:
+            raise ValueError("state has %d elements, solver needs %d" % (a.size, self.count))
+        check(lib().hgpu_set_state(self.h, a.ctypes.data, a.size))
+
+    set_state = resetState
+
+    def getState(self, out=None):
+        a = out if out is not None else np.empty(self.count, dtype=self.dtype)
+        check(lib().hgpu_get_state(self.h, a.ctypes.data, a.size))
+        return a
+
+    get_state = getState
+
+    def update(self, nsteps=1, want_dt=True):
+        dt = ctypes.c_double()
+        check(lib().hgpu_update(self.h, int(nsteps), ctypes.byref(dt) if want_dt else None))
+        self.frame += nsteps
+        return dt.value if want_dt else None
+
+    def last_dt(self):
+        dt = ctypes.c_double()
+        check(lib().hgpu_last_dt(self.h, ctypes.byref(dt)))
+        return dt.value
+
+    def synchronize(self):
+        check(lib().hgpu_synchronize(self.h))
+
+    def health(self):
+        f = ctypes.c_uint32()
+        check(lib().hgpu_health(self.h, ctypes.byref(f)))
+        return f.value
+
+    def set_graphs(self, on):
+        check(lib().hgpu_set_graphs(self.h, 1 if on else 0))
+
+    def kernels_per_step(self):
+        n = ctypes.c_int()
+        check(lib().hgpu_kernels_per_step(self.h, ctypes.byref(n)))
+        return n.value
+
+    def timed_update(self, nsteps):
+        """Run nsteps and return their device time in ms (CUDA events on the solver stream)."""
+        ms = ctypes.c_float()
+        check(lib().hgpu_timed_update(self.h, int(nsteps), ctypes.byref(ms)))
+        self.frame += nsteps
+        return ms.value
+
+    def profile(self, nsteps=1):
+        """Per-kernel device times of nsteps plain-launch updates: {name: (launches, total_ms)}."""
+        arr = (KernelTime * 32)()
+        n = ctypes.c_int()
+        check(lib().hgpu_profile_update(self.h, int(nsteps), ctypes.cast(arr, ctypes.c_void_p), 32, ctypes.byref(n)))
+        self.frame += nsteps
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(min(n.value, 32))}
+
+    def state_device_ptr(self):
+        p = ctypes.c_void_p()
+        check(lib().hgpu_state_device_ptr(self.h, ctypes.byref(p)))
+        return p.value
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        check(lib().hgpu_stream(self.h, ctypes.byref(p)))
+        return p.value
+
+    def save(self, prefix):
+        """Solver::save (src/Solver/Solver.cpp:563-589) without the FITS dependency:
+        one little-endian raw file per state channel, <prefix><STATE>.raw, plus
+        <prefix>header.json describing sizes and dtype."""
+        import json
+        names = ["DENSITY", "MOMENTUM_X", "MOMENTUM_Y", "MOMENTUM_Z"][: 1 + self.dim] + ["ENERGY_TOTAL"]
+        st = self.getState().reshape(self.shape())
+        for j, n in enumerate(names):
+            np.ascontiguousarray(st[..., j]).astype("<" + np.dtype(self.dtype).str[1:]).tofile(prefix + n + ".raw")
+        with open(prefix + "header.json", "w") as f:
+            json.dump({"size": list(self.cfg.size), "dtype": np.dtype(self.dtype).name, "channels": names,
+                       "frame": self.frame}, f)
+        return names

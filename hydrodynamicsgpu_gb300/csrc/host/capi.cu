@@ -1,0 +1,311 @@
+// capi.cu -- the extern "C" boundary declared in include/hgpu/hgpu.h.
+// No C++ exception crosses it: every entry point maps failures to an hgpu_status
+// and keeps a per-thread message for hgpu_last_error().
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "solver.h"
+
+namespace hgpu {
+double measureFp64FmaRate();
+}
+
+struct hgpu_solver {
+    std::unique_ptr<hgpu::SolverBase> s;
+    bool graphs = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    int kernelsPerStep = 0;
+};
+
+namespace {
+thread_local std::string g_lastError;
+
+int fail(int status, const std::string& msg) {
+    g_lastError = msg;
+    return status;
+}
+
+template <class F>
+int guarded(F f) {
+    try {
+        return f();
+    } catch (const hgpu::ConfigError& e) {
+        return fail(e.status, e.what());
+    } catch (const hgpu::CudaError& e) {
+        return fail(e.code == cudaErrorMemoryAllocation ? HGPU_ERR_NOMEM : HGPU_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(HGPU_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(HGPU_ERR_CUDA, e.what());
+    }
+}
+
+void runSteps(hgpu_solver* h, int nsteps);
+
+void destroyGraph(hgpu_solver* h) {
+    if (h->exec) cudaGraphExecDestroy(h->exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->exec = nullptr;
+    h->graph = nullptr;
+}
+
+void captureStep(hgpu_solver* h) {
+    cudaStream_t st = h->s->stream;
+    hgpu::cudaCheck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    try {
+        h->s->update();
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    hgpu::cudaCheck(cudaStreamEndCapture(st, &h->graph), "end capture");
+    hgpu::cudaCheck(cudaGraphInstantiate(&h->exec, h->graph, 0), "graph instantiate");
+    h->kernelsPerStep = h->s->kernelsPerStep();
+}
+void runSteps(hgpu_solver* h, int nsteps) {
+    for (int i = 0; i < nsteps; ++i) {
+        if (h->graphs) {
+            if (!h->exec) captureStep(h);
+            hgpu::cudaCheck(cudaGraphLaunch(h->exec, h->s->stream), "graph launch");
+        } else {
+            h->s->update();
+            h->kernelsPerStep = h->s->kernelsPerStep();
+            hgpu::cudaCheck(cudaGetLastError(), "kernel launch");
+        }
+    }
+}
+}  // namespace
+
+extern "C" {
+
+const char* hgpu_last_error(void) { return g_lastError.c_str(); }
+
+const char* hgpu_status_string(int status) {
+    switch (status) {
+    case HGPU_OK: return "HGPU_OK";
+    case HGPU_ERR_CONFIG: return "HGPU_ERR_CONFIG";
+    case HGPU_ERR_CUDA: return "HGPU_ERR_CUDA";
+    case HGPU_ERR_NONFINITE: return "HGPU_ERR_NONFINITE";
+    case HGPU_ERR_TIMEOUT: return "HGPU_ERR_TIMEOUT";
+    case HGPU_ERR_OOB: return "HGPU_ERR_OOB";
+    case HGPU_ERR_ARG: return "HGPU_ERR_ARG";
+    case HGPU_ERR_UNSUPPORTED: return "HGPU_ERR_UNSUPPORTED";
+    case HGPU_ERR_NOMEM: return "HGPU_ERR_NOMEM";
+    }
+    return "HGPU_ERR_UNKNOWN";
+}
+
+int hgpu_config_default(hgpu_config* cfg) {
+    if (!cfg) return fail(HGPU_ERR_ARG, "null config");
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->solver = HGPU_SOLVER_ROE;
+    cfg->dim = 0;
+    cfg->size[0] = 256; cfg->size[1] = 256; cfg->size[2] = 1;
+    for (int i = 0; i < 3; ++i) { cfg->xmin[i] = -.5; cfg->xmax[i] = .5; }
+    cfg->gamma = 1.4;
+    cfg->cfl = .5f;
+    cfg->use_fixed_dt = 0;
+    cfg->fixed_dt = .001;
+    for (int i = 0; i < 3; ++i) { cfg->boundary[i][0] = HGPU_BOUNDARY_FREEFLOW; cfg->boundary[i][1] = HGPU_BOUNDARY_FREEFLOW; }
+    cfg->limiter = HGPU_LIMITER_SUPERBEE;
+    cfg->integrator = HGPU_INTEGRATOR_FORWARD_EULER;
+    cfg->precision = HGPU_FP64;
+    cfg->compat = HGPU_COMPAT_REF;
+    return HGPU_OK;
+}
+
+int hgpu_create(const hgpu_config* cfg, hgpu_solver** out) {
+    if (!cfg || !out) return fail(HGPU_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&]() {
+        std::unique_ptr<hgpu_solver> h(new hgpu_solver());
+        h->s = hgpu::createSolver(*cfg);
+        *out = h.release();
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_destroy(hgpu_solver* h) {
+    if (!h) return HGPU_OK;
+    return guarded([&]() {
+        if (h->s && h->s->stream) cudaStreamSynchronize(h->s->stream);
+        destroyGraph(h);
+        if (h->t0) cudaEventDestroy(h->t0);
+        if (h->t1) cudaEventDestroy(h->t1);
+        delete h;
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_get_shape(const hgpu_solver* h, int* dim, int* num_states, size_t* volume) {
+    if (!h) return fail(HGPU_ERR_ARG, "null handle");
+    if (dim) *dim = h->s->dim();
+    if (num_states) *num_states = h->s->numStates();
+    if (volume) *volume = h->s->volume();
+    return HGPU_OK;
+}
+
+int hgpu_set_state(hgpu_solver* h, const void* host_state, size_t count) {
+    if (!h || !host_state) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { h->s->resetState(host_state, count); return (int)HGPU_OK; });
+}
+
+int hgpu_get_state(hgpu_solver* h, void* host_state, size_t count) {
+    if (!h || !host_state) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { h->s->readState(host_state, count); return (int)HGPU_OK; });
+}
+
+int hgpu_update(hgpu_solver* h, int nsteps, double* last_dt) {
+    if (!h || nsteps < 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        runSteps(h, nsteps);
+        if (last_dt) *last_dt = h->s->lastDt();
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_last_dt(hgpu_solver* h, double* dt) {
+    if (!h || !dt) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { *dt = h->s->lastDt(); return (int)HGPU_OK; });
+}
+
+int hgpu_synchronize(hgpu_solver* h) {
+    if (!h) return fail(HGPU_ERR_ARG, "null handle");
+    return guarded([&]() {
+        hgpu::cudaCheck(cudaStreamSynchronize(h->s->stream), "synchronize");
+        unsigned flags = 0;
+        hgpu::cudaCheck(cudaMemcpy(&flags, h->s->health, sizeof flags, cudaMemcpyDeviceToHost), "health read");
+        if (flags & hgpu::HEALTH_NONFINITE_DT) return fail(HGPU_ERR_NONFINITE, "non-finite value in the CFL reduction");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_health(hgpu_solver* h, uint32_t* flags) {
+    if (!h || !flags) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        unsigned f = 0;
+        hgpu::cudaCheck(cudaStreamSynchronize(h->s->stream), "synchronize");
+        hgpu::cudaCheck(cudaMemcpy(&f, h->s->health, sizeof f, cudaMemcpyDeviceToHost), "health read");
+        hgpu::cudaCheck(cudaMemset(h->s->health, 0, sizeof f), "health clear");
+        *flags = f;
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_state_device_ptr(hgpu_solver* h, void** dptr) {
+    if (!h || !dptr) return fail(HGPU_ERR_ARG, "null argument");
+    *dptr = h->s->stateDevicePtr();
+    return HGPU_OK;
+}
+
+int hgpu_stream(hgpu_solver* h, void** stream) {
+    if (!h || !stream) return fail(HGPU_ERR_ARG, "null argument");
+    *stream = (void*)h->s->stream;
+    return HGPU_OK;
+}
+
+int hgpu_set_graphs(hgpu_solver* h, int enabled) {
+    if (!h) return fail(HGPU_ERR_ARG, "null handle");
+    return guarded([&]() {
+        h->graphs = enabled != 0;
+        if (!h->graphs) destroyGraph(h);
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_kernels_per_step(const hgpu_solver* h, int* count) {
+    if (!h || !count) return fail(HGPU_ERR_ARG, "null argument");
+    *count = h->kernelsPerStep;
+    return HGPU_OK;
+}
+
+int hgpu_select_device(int device) {
+    return guarded([&]() {
+        hgpu::cudaCheck(cudaSetDevice(device), "cudaSetDevice");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_timed_update(hgpu_solver* h, int nsteps, float* ms) {
+    if (!h || !ms || nsteps < 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        if (!h->t0) {
+            hgpu::cudaCheck(cudaEventCreate(&h->t0), "event create");
+            hgpu::cudaCheck(cudaEventCreate(&h->t1), "event create");
+        }
+        if (h->graphs && !h->exec) captureStep(h);
+        hgpu::cudaCheck(cudaEventRecord(h->t0, h->s->stream), "event record");
+        runSteps(h, nsteps);
+        hgpu::cudaCheck(cudaEventRecord(h->t1, h->s->stream), "event record");
+        hgpu::cudaCheck(cudaEventSynchronize(h->t1), "event sync");
+        hgpu::cudaCheck(cudaEventElapsedTime(ms, h->t0, h->t1), "elapsed");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_profile_update(hgpu_solver* h, int nsteps, hgpu_kernel_time* out, int cap, int* count) {
+    if (!h || nsteps < 0 || (cap > 0 && !out)) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        hgpu::SolverBase* s = h->s.get();
+        s->records.clear();
+        s->eventNext = 0;
+        s->profiling = true;
+        try {
+            for (int i = 0; i < nsteps; ++i) s->update();
+        } catch (...) {
+            s->profiling = false;
+            throw;
+        }
+        s->profiling = false;
+        hgpu::cudaCheck(cudaStreamSynchronize(s->stream), "profile sync");
+        std::vector<hgpu_kernel_time> agg;
+        for (const auto& r : s->records) {
+            float ms = 0;
+            hgpu::cudaCheck(cudaEventElapsedTime(&ms, r.start, r.stop), "elapsed");
+            size_t k = 0;
+            for (; k < agg.size(); ++k)
+                if (!std::strncmp(agg[k].name, r.kind, sizeof agg[k].name)) break;
+            if (k == agg.size()) {
+                hgpu_kernel_time t{};
+                std::strncpy(t.name, r.kind, sizeof t.name - 1);
+                agg.push_back(t);
+            }
+            agg[k].launches += 1;
+            agg[k].total_ms += ms;
+        }
+        int n = (int)agg.size();
+        for (int i = 0; i < n && i < cap; ++i) out[i] = agg[i];
+        if (count) *count = n;
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        hgpu::cudaCheck(cudaHostAlloc(ptr, bytes, cudaHostAllocPortable), "cudaHostAlloc");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_host_free(void* ptr) {
+    return guarded([&]() {
+        if (ptr) hgpu::cudaCheck(cudaFreeHost(ptr), "cudaFreeHost");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_fp64_peak(double* fma_per_second) {
+    if (!fma_per_second) return fail(HGPU_ERR_ARG, "null argument");
+    double r = hgpu::measureFp64FmaRate();
+    if (r <= 0) return fail(HGPU_ERR_CUDA, "fp64 probe failed");
+    *fma_per_second = r;
+    return HGPU_OK;
+}
+
+}  // extern "C"

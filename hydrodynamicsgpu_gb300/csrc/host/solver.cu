@@ -1,0 +1,496 @@
+// solver.cu -- host side of the GB300 Euler update: configuration, buffers, the
+// step sequence and the Runge-Kutta stage plans.  Host code only (built by nvcc
+// so the launchers' CUDA types resolve); the kernels live in ../kernels/.
+#include "solver.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+
+namespace hgpu {
+
+void cudaCheck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(e, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DeviceBuffer::DeviceBuffer(size_t bytes, bool zero) : bytes_(bytes) {
+    if (bytes == 0) return;
+    cudaError_t e = cudaMalloc(&ptr_, bytes);
+    if (e != cudaSuccess) {
+        ptr_ = nullptr;
+        (void)cudaGetLastError();
+        throw CudaError(e, "cudaMalloc of " + std::to_string(bytes) + " bytes");
+    }
+    if (zero) cudaCheck(cudaMemset(ptr_, 0, bytes), "cudaMemset");
+}
+
+DeviceBuffer::~DeviceBuffer() {
+    if (ptr_) cudaFree(ptr_);
+}
+
+DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
+    if (this != &o) {
+        if (ptr_) cudaFree(ptr_);
+        ptr_ = o.ptr_; bytes_ = o.bytes_;
+        o.ptr_ = nullptr; o.bytes_ = 0;
+    }
+    return *this;
+}
+
+SolverBase::~SolverBase() {
+    for (cudaEvent_t e : eventPool) cudaEventDestroy(e);
+}
+
+cudaEvent_t SolverBase::eventFromPool() {
+    if (eventNext == eventPool.size()) {
+        cudaEvent_t e;
+        cudaCheck(cudaEventCreate(&e), "cudaEventCreate");
+        eventPool.push_back(e);
+    }
+    return eventPool[eventNext++];
+}
+
+// ---------------- configuration ----------------
+// toNumericString<double> (include/HydroGPU/toNumericString.h:12-22): ostream default
+// formatting, i.e. 6 significant digits.
+static double bakedDx(double v) {
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%g", v);
+    return std::strtod(buf, nullptr);
+}
+
+ResolvedConfig resolveConfig(const hgpu_config& cfg) {
+    ResolvedConfig rc;
+    rc.cfg = cfg;
+    int dim = cfg.dim;
+    if (dim == 0) {                                   // HydroGPUApp.cpp:214-221
+        for (dim = 3; dim > 0; --dim)
+            if (cfg.size[dim - 1] > 1) break;
+    }
+    if (dim < 1 || dim > 3) throw ConfigError(HGPU_ERR_CONFIG, "could not determine the dimension from size");
+    for (int i = 0; i < 3; ++i) {
+        if (i < dim && cfg.size[i] < 5) throw ConfigError(HGPU_ERR_CONFIG, "size must be >= 5 on every active axis");
+        if (i >= dim && cfg.size[i] != 1) throw ConfigError(HGPU_ERR_CONFIG, "size must be 1 beyond dim");
+    }
+    if (cfg.solver != HGPU_SOLVER_ROE && cfg.solver != HGPU_SOLVER_HLLC)
+        throw ConfigError(HGPU_ERR_CONFIG, "unknown solver");
+    if (cfg.limiter < 0 || cfg.limiter >= HGPU_NUM_LIMITERS) throw ConfigError(HGPU_ERR_CONFIG, "unknown slope limiter");
+    if (cfg.integrator < 0 || cfg.integrator >= HGPU_NUM_INTEGRATORS)
+        throw ConfigError(HGPU_ERR_CONFIG, "unknown integrator");
+    if (cfg.precision != HGPU_FP64 && cfg.precision != HGPU_FP32) throw ConfigError(HGPU_ERR_CONFIG, "unknown precision");
+    if (cfg.compat != HGPU_COMPAT_REF && cfg.compat != HGPU_COMPAT_SEAM)
+        throw ConfigError(HGPU_ERR_CONFIG, "unknown compat mode");
+    for (int i = 0; i < dim; ++i)
+        for (int m = 0; m < 2; ++m) {
+            int b = cfg.boundary[i][m];
+            if (b < HGPU_BOUNDARY_NONE || b > HGPU_BOUNDARY_FREEFLOW)
+                throw ConfigError(HGPU_ERR_CONFIG, "unknown boundary method");
+        }
+    if (!(cfg.gamma > 1.0)) throw ConfigError(HGPU_ERR_CONFIG, "gamma must be > 1");
+    if (!(cfg.cfl > 0.f)) throw ConfigError(HGPU_ERR_CONFIG, "cfl must be > 0");
+    if (cfg.use_fixed_dt && !(cfg.fixed_dt > 0)) throw ConfigError(HGPU_ERR_CONFIG, "fixed_dt must be > 0");
+    // dx = (xmax - xmin) / (float)size, in the program's real type (HydroGPUApp.cpp:224-226)
+    for (int i = 0; i < 3; ++i) {
+        double d;
+        if (cfg.precision == HGPU_FP32)
+            d = (double)(((float)cfg.xmax[i] - (float)cfg.xmin[i]) / (float)cfg.size[i]);
+        else
+            d = (cfg.xmax[i] - cfg.xmin[i]) / (double)(float)cfg.size[i];
+        rc.dx[i] = cfg.compat == HGPU_COMPAT_REF ? bakedDx(d) : d;
+        if (i < dim && !(rc.dx[i] > 0)) throw ConfigError(HGPU_ERR_CONFIG, "xmax must exceed xmin");
+    }
+    // `defs` values reach the program through Lua's number formatting (%.14g)
+    if (cfg.compat == HGPU_COMPAT_REF) {
+        char buf[64];
+        std::snprintf(buf, sizeof buf, "%.14g", cfg.gamma);
+        rc.gamma = std::strtod(buf, nullptr);
+    } else {
+        rc.gamma = cfg.gamma;
+    }
+    rc.dim = dim;
+    rc.numStates = dim + 2;
+    Grid& g = rc.grid;
+    for (int i = 0; i < 3; ++i) g.S[i] = cfg.size[i];
+    g.dim = dim;
+    g.step[0] = 1;
+    g.step[1] = cfg.size[0];
+    g.step[2] = (long long)cfg.size[0] * cfg.size[1];
+    g.V = (long long)cfg.size[0] * cfg.size[1] * cfg.size[2];
+    return rc;
+}
+
+// ---------------- Equation ----------------
+Euler::Euler(const hgpu_config& cfg, int dim) : cfg_(cfg) {      // src/Equation/Euler.cpp:12-49
+    boundaryMethods = {"PERIODIC", "MIRROR", "FREEFLOW"};
+    states.push_back("DENSITY");
+    states.push_back("MOMENTUM_X");
+    if (dim > 1) states.push_back("MOMENTUM_Y");
+    if (dim > 2) states.push_back("MOMENTUM_Z");
+    states.push_back("ENERGY_TOTAL");
+}
+
+int Euler::stateGetBoundaryKernelForBoundaryMethod(int dim, int state, int minmax) const {   // Euler.cpp:63-75
+    switch (cfg_.boundary[dim][minmax]) {
+    case HGPU_BOUNDARY_NONE: return -1;
+    case HGPU_BOUNDARY_PERIODIC: return 0;
+    case HGPU_BOUNDARY_MIRROR: return dim + 1 == state ? 2 : 1;
+    case HGPU_BOUNDARY_FREEFLOW: return 3;
+    }
+    throw ConfigError(HGPU_ERR_CONFIG, "unknown boundary method");
+}
+
+// ---------------- Integrators ----------------
+template <typename real>
+void ForwardEuler<real>::integrate(const std::function<void(real* stage)>& computeFlux) {
+    Solver<real>* s = this->solver;
+    computeFlux(s->state.template as<real>());
+    CombinePlan<real> plan{};
+    plan.fe = 1;
+    plan.slot[0] = s->state.template as<real>();
+    s->launch("flux_divergence_combine", 1, [&] {
+        launchDerivCombine<real>(s->rc.grid, s->ph, s->flux.template as<real>(), plan, s->sc(), s->stream);
+    });
+}
+
+template <typename real>
+void ForwardEuler<real>::integrateZeroDeriv() {
+    Solver<real>* s = this->solver;
+    s->boundary();                                            // the callback's solver->boundary()
+    s->launch("gravity_pass", 1, [&] { launchZeroAdd<real>(s->rc.grid, s->state.template as<real>(), s->sc(), s->stream); });
+}
+
+template <typename real>
+RungeKutta<real>::RungeKutta(Solver<real>* s, int tableau) : Integrator<real>(s), tableau_(tableau) {
+    order_ = tableauOrder(tableau);
+    for (int m = 0; m < order_; ++m)
+        for (int k = 0; k <= m; ++k) {
+            double a = tableauAlpha(tableau, m, k);
+            if (a != 0.0 && a != 1.0) alphaIsBinary_ = false;
+        }
+    buildPlans();
+}
+
+// Build the per-stage combine plans.  Row m of the tableau (the input of stage m+1,
+// or the new state for m = order-1) is accumulated column by column: at stage k
+// its alpha(m,k) u^(k) and beta(m,k) dt d^(k) terms are added, in that order, to its
+// partial sum.  A row whose sum is still exactly u^n (alpha = 1, nothing else) is
+// not materialised: it aliases the state buffer, which holds u^n until the last
+// stage writes the new state into it.
+template <typename real>
+void RungeKutta<real>::buildPlans() {
+    const int order = order_;
+    struct Row { int slot = -1; bool alias0 = false; };
+    std::vector<Row> rows(order);
+    std::vector<bool> slotBusy(8, false);
+    slotBusy[0] = true;
+    int maxSlot = 0;
+    auto alloc = [&]() {
+        for (int i = 1; i < 8; ++i)
+            if (!slotBusy[i]) { slotBusy[i] = true; maxSlot = std::max(maxSlot, i); return i; }
+        throw std::logic_error("out of Runge-Kutta work slots");
+    };
+    int inSlot = 0;
+    plans_.clear();
+    inputSlot_.clear();
+    for (int k = 0; k < order; ++k) {
+        CombinePlan<real> plan{};
+        plan.fe = 0;
+        plan.in = inSlot;
+        for (int m = k; m < order; ++m) {
+            double a = tableauAlpha(tableau_, m, k), b = tableauBeta(tableau_, m, k);
+            if (a == 0.0 && b == 0.0) continue;
+            Row& r = rows[m];
+            bool fresh = r.slot < 0 && !r.alias0;
+            if (fresh && a == 1.0 && b == 0.0 && inSlot == 0 && !(m == order - 1 && k == order - 1)) {
+                r.alias0 = true;           // sum so far == +0 + u^n * 1
+                continue;
+            }
+            CombineOp<real> op{};
+            op.prior = r.alias0 ? 0 : r.slot;
+            op.priorAlias = r.alias0 ? 1 : 0;
+            op.hasAlpha = a != 0.0;
+            op.alpha = (real)a;
+            op.alphaIsOne = a == 1.0;
+            op.hasBeta = b != 0.0;
+            op.brow = m;
+            op.bcol = k;
+            if (m == order - 1 && k == order - 1) op.out = 0;
+            else if (r.slot >= 0) op.out = r.slot;
+            else op.out = alloc();
+            r.slot = op.out;
+            r.alias0 = false;
+            if (plan.nops >= 4) throw std::logic_error("too many rows in a stage");
+            plan.ops[plan.nops++] = op;
+        }
+        plans_.push_back(plan);
+        inputSlot_.push_back(inSlot);
+        if (k < order - 1) {
+            if (inSlot != 0) slotBusy[inSlot] = false;   // u^(k) is consumed by stage k
+            inSlot = rows[k].alias0 ? 0 : rows[k].slot;
+        }
+    }
+    nslots_ = maxSlot;
+    work_.clear();
+    size_t bytes = sizeof(real) * (size_t)this->solver->rc.grid.V * this->solver->rc.numStates;
+    for (int i = 0; i < nslots_; ++i) work_.emplace_back(bytes, true);
+    for (auto& p : plans_) {
+        p.slot[0] = this->solver->state.template as<real>();
+        for (int i = 0; i < nslots_; ++i) p.slot[1 + i] = work_[i].template as<real>();
+    }
+}
+
+template <typename real>
+void RungeKutta<real>::integrate(const std::function<void(real* stage)>& computeFlux) {
+    Solver<real>* s = this->solver;
+    for (int k = 0; k < order_; ++k) {
+        real* in = plans_[k].slot[inputSlot_[k]];
+        computeFlux(in);
+        s->launch("flux_divergence_combine", 1, [&] {
+            launchDerivCombine<real>(s->rc.grid, s->ph, s->flux.template as<real>(), plans_[k], s->sc(), s->stream);
+        });
+    }
+}
+
+template <typename real>
+void RungeKutta<real>::integrateZeroDeriv() {
+    // With every deriv +0 the stage states are alpha-combinations of u^n.  For
+    // tableaus whose alphas are all 0 or 1 that is u^n itself (the step leaves no -0
+    // in the state), so nothing runs.
+    if (alphaIsBinary_) return;
+    Solver<real>* s = this->solver;
+    s->launch("gravity_pass", 1, [&] {
+        launchAlphaOnly<real>(s->rc.grid, tableau_, s->state.template as<real>(), s->sc(), s->stream);
+    });
+}
+
+// ---------------- Solver ----------------
+template <typename real>
+Solver<real>::Solver(const ResolvedConfig& rc_) : rc(rc_) {
+    for (int i = 0; i < 3; ++i) ph.dx[i] = (real)rc.dx[i];
+    ph.gamma = (real)rc.gamma;
+    ph.cfl = rc.cfg.cfl;
+}
+
+template <typename real>
+Solver<real>::~Solver() {
+    integrator.reset();
+    if (stream) cudaStreamDestroy(stream);
+}
+
+template <typename real>
+unsigned long long Solver<real>::accInit() const {
+    // Roe writes every dtBuffer entry (INFINITY outside the interior); HLLC writes only
+    // the first volume entries, the rest keep their initial max() (Solver.cpp:217-222,
+    // EulerHLLC.cl:135-168), which joins the minimum when dim > 1.
+    bool maxInit = rc.cfg.solver == HGPU_SOLVER_HLLC && rc.dim > 1;
+    if (sizeof(real) == 8) {
+        double v = maxInit ? DBL_MAX : std::numeric_limits<double>::infinity();
+        unsigned long long b;
+        std::memcpy(&b, &v, 8);
+        return b;
+    }
+    float v = maxInit ? FLT_MAX : std::numeric_limits<float>::infinity();
+    unsigned int b;
+    std::memcpy(&b, &v, 4);
+    return b;
+}
+
+template <typename real>
+void Solver<real>::init() {                                  // Solver::init (Solver.cpp:48-205)
+    equation.reset(new Euler(rc.cfg, rc.dim));
+    cudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (int i = 0; i < 3; ++i)
+        for (int m = 0; m < 2; ++m) methods[i][m] = i < rc.dim ? rc.cfg.boundary[i][m] : -1;
+    initBuffers();
+    if (rc.cfg.integrator == HGPU_INTEGRATOR_FORWARD_EULER) integrator.reset(new ForwardEuler<real>(this));
+    else integrator.reset(new RungeKutta<real>(this, rc.cfg.integrator));
+    unsigned long long init = accInit();
+    cudaCheck(cudaMemcpy(dtAcc.get(), &init, sizeof init, cudaMemcpyHostToDevice), "dt accumulator init");
+    cudaCheck(cudaDeviceSynchronize(), "init");
+}
+
+template <typename real>
+void Solver<real>::initBuffers() {                           // Solver::initBuffers (Solver.cpp:208-223)
+    size_t n = (size_t)rc.grid.V * rc.numStates;
+    state = DeviceBuffer(sizeof(real) * n, true);
+    stepConst = DeviceBuffer(sizeof(StepConst<real>), true);
+    dtAcc = DeviceBuffer(sizeof(unsigned long long), true);
+    healthBuf = DeviceBuffer(sizeof(unsigned), true);
+    health = healthBuf.as<unsigned>();
+}
+
+template <typename real>
+void Solver<real>::resetState(const void* host, size_t count) {
+    if (count != (size_t)rc.grid.V * rc.numStates) throw ConfigError(HGPU_ERR_ARG, "state element count mismatch");
+    cudaCheck(cudaMemcpyAsync(state.get(), host, sizeof(real) * count, cudaMemcpyHostToDevice, stream), "set_state");
+    cudaCheck(cudaStreamSynchronize(stream), "set_state sync");
+}
+
+template <typename real>
+void Solver<real>::readState(void* host, size_t count) {
+    if (count != (size_t)rc.grid.V * rc.numStates) throw ConfigError(HGPU_ERR_ARG, "state element count mismatch");
+    cudaCheck(cudaMemcpyAsync(host, state.get(), sizeof(real) * count, cudaMemcpyDeviceToHost, stream), "get_state");
+    cudaCheck(cudaStreamSynchronize(stream), "get_state sync");
+}
+
+template <typename real>
+double Solver<real>::lastDt() {
+    double dt = 0;
+    cudaCheck(cudaMemcpyAsync(&dt, &sc()->dt_f64, sizeof dt, cudaMemcpyDeviceToHost, stream), "last dt");
+    cudaCheck(cudaStreamSynchronize(stream), "last dt sync");
+    return dt;
+}
+
+template <typename real>
+void Solver<real>::boundaryOn(real* buf) {
+    launch("boundary", rc.dim, [&] { launchBoundary<real>(rc.grid, methods, buf, stream); });
+}
+
+template <typename real>
+void Solver<real>::boundary() { boundaryOn(state.as<real>()); }
+
+template <typename real>
+void Solver<real>::finalizeDt(bool fixed) {
+    launch("finalize_dt", 1, [&] {
+        launchFinalizeDt<real>(ph, rc.cfg.integrator, fixed ? 1 : 0, rc.cfg.fixed_dt, dtAcc.as<unsigned long long>(),
+                               accInit(), sc(), health, stream);
+    });
+}
+
+template <typename real>
+void Solver<real>::update() {                                // Solver::update (Solver.cpp:521-546)
+    this->launches_ = 0;
+    boundary();
+    initStep();
+    if (rc.cfg.use_fixed_dt) finalizeDt(true);
+    else {
+        calcTimestep();
+        finalizeDt(false);
+    }
+    step();
+}
+
+template <typename real>
+void Solver<real>::applyPotential() { integrator->integrateZeroDeriv(); }
+
+template <typename real>
+void FiniteVolumeSolver<real>::initBuffers() {               // FiniteVolumeSolver.cpp:10-15
+    Solver<real>::initBuffers();
+    this->flux = DeviceBuffer(sizeof(real) * (size_t)this->rc.grid.V * this->rc.numStates * this->rc.dim, true);
+}
+
+template <typename real>
+void Roe<real>::initBuffers() {                              // Roe.cpp:11-16 (compact basis record)
+    FiniteVolumeSolver<real>::initBuffers();
+    const auto& rc = this->rc;
+    basis = DeviceBuffer(sizeof(real) * (size_t)rc.grid.V * rc.dim * roeRecordSize(rc.dim), true);
+    deltaQTilde = DeviceBuffer(sizeof(real) * (size_t)rc.grid.V * rc.dim * rc.numStates, true);
+}
+
+template <typename real>
+void Roe<real>::initFlux() {                                 // Roe::initFlux (Roe.cpp:82-86)
+    this->launch("roe_eigenbasis", 1, [&] {
+        launchRoeBasis<real>(this->rc.grid, this->ph, this->state.template as<real>(), basis.template as<real>(),
+                             this->rc.cfg.compat == HGPU_COMPAT_SEAM, this->stream);
+    });
+}
+
+template <typename real>
+void Roe<real>::calcTimestep() {                             // Roe::calcTimestep (Roe.cpp:88-92)
+    initFlux();
+    this->launch("cfl_min_reduce", 1, [&] {
+        launchRoeDt<real>(this->rc.grid, this->ph, basis.template as<real>(),
+                          this->dtAcc.template as<unsigned long long>(), this->health, this->stream);
+    });
+}
+
+template <typename real>
+void Roe<real>::calcFlux(real* stage) {                      // Roe::calcDeriv (Roe.cpp:101-112)
+    bool seam = this->rc.cfg.compat == HGPU_COMPAT_SEAM;
+    if (seam && stage != this->state.template as<real>()) this->boundaryOn(stage);
+    this->launch("roe_delta_q_tilde", 1, [&] {
+        launchRoeDeltaQ<real>(this->rc.grid, stage, basis.template as<real>(), deltaQTilde.template as<real>(), seam,
+                              this->stream);
+    });
+    this->launch("roe_flux", 1, [&] {
+        launchRoeFlux<real>(this->rc.grid, this->rc.cfg.limiter, stage, basis.template as<real>(),
+                            deltaQTilde.template as<real>(), this->sc(), this->flux.template as<real>(), seam,
+                            this->stream);
+    });
+}
+
+template <typename real>
+void Roe<real>::step() {                                     // Roe::step (Roe.cpp:94-99)
+    this->integrator->integrate([this](real* stage) { calcFlux(stage); });
+}
+
+template <typename real>
+void EulerRoe<real>::step() {                                // EulerRoe::step (EulerRoe.cpp:31-34)
+    Roe<real>::step();
+    this->applyPotential();
+}
+
+template <typename real>
+void HLL<real>::initBuffers() {                              // HLL.cpp:7-11 (sl, sr per face)
+    FiniteVolumeSolver<real>::initBuffers();
+    waves = DeviceBuffer(sizeof(real) * (size_t)this->rc.grid.V * this->rc.dim * 2, true);
+}
+
+template <typename real>
+void HLL<real>::initStep() {                                 // HLL::initStep (HLL.cpp:31-33)
+    this->launch("hllc_wave_speeds", 1, [&] {
+        launchHllcWaves<real>(this->rc.grid, this->ph, this->state.template as<real>(), waves.template as<real>(),
+                              this->stream);
+    });
+}
+
+template <typename real>
+void HLL<real>::calcTimestep() {                             // HLL::calcTimestep (HLL.cpp:35-38)
+    this->launch("cfl_min_reduce", 1, [&] {
+        launchHllcDt<real>(this->rc.grid, this->ph, waves.template as<real>(),
+                           this->dtAcc.template as<unsigned long long>(), this->health, this->stream);
+    });
+}
+
+template <typename real>
+void HLL<real>::step() {                                     // HLL::step (HLL.cpp:40-47)
+    this->integrator->integrate([this](real* stage) {
+        this->launch("hllc_flux", 1, [&] {
+            launchHllcFlux<real>(this->rc.grid, this->ph, stage, waves.template as<real>(),
+                                 this->flux.template as<real>(), this->health, this->stream);
+        });
+    });
+}
+
+template <typename real>
+void EulerHLL<real>::step() {                                // EulerHLL::step (EulerHLL.cpp:25-28)
+    HLL<real>::step();
+    this->applyPotential();
+}
+
+template <typename real>
+static std::unique_ptr<SolverBase> makeSolver(const ResolvedConfig& rc) {
+    std::unique_ptr<SolverBase> s;
+    if (rc.cfg.solver == HGPU_SOLVER_ROE) s.reset(new EulerRoe<real>(rc));
+    else s.reset(new EulerHLLC<real>(rc));
+    s->init();
+    return s;
+}
+
+std::unique_ptr<SolverBase> createSolver(const hgpu_config& cfg) {
+    ResolvedConfig rc = resolveConfig(cfg);
+    if (cfg.precision == HGPU_FP32) return makeSolver<float>(rc);
+    return makeSolver<double>(rc);
+}
+
+template class Solver<double>;
+template class Solver<float>;
+template class ForwardEuler<double>;
+template class ForwardEuler<float>;
+template class RungeKutta<double>;
+template class RungeKutta<float>;
+
+}  // namespace hgpu

@@ -1,0 +1,274 @@
+// solver.h -- C++ host classes of the GB300 Euler update, mirroring HydroGPU's
+// Solver / Equation / Integrator hierarchy (include/HydroGPU/Solver/*.h,
+// include/HydroGPU/Equation/*.h, include/HydroGPU/Integrator/*.h).
+//
+// Differences from the reference that the GB300 design introduces:
+//  * buffers are CUDA device allocations owned by the solver (DeviceBuffer);
+//  * the timestep is reduced and kept on the device; update() never blocks;
+//  * Integrator::integrate's callback receives the stage state and produces the
+//    interface fluxes of that stage; the integrator's fused kernel turns them into
+//    the flux divergence and folds it into every Runge-Kutta row that needs it.
+#pragma once
+#include <cuda_runtime.h>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/hgpu/hgpu.h"
+#include "../kernels/kernels.h"
+
+namespace hgpu {
+
+struct CudaError : std::runtime_error {
+    cudaError_t code;
+    CudaError(cudaError_t c, const std::string& what) : std::runtime_error(what), code(c) {}
+};
+void cudaCheck(cudaError_t e, const char* what);
+
+struct ConfigError : std::runtime_error {
+    int status;
+    ConfigError(int s, const std::string& what) : std::runtime_error(what), status(s) {}
+};
+
+// owning device allocation (replaces cl::Buffer, Solver::CL::alloc/zero: Solver.cpp:17-38)
+class DeviceBuffer {
+public:
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(size_t bytes, bool zero = true);
+    ~DeviceBuffer();
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) { o.ptr_ = nullptr; o.bytes_ = 0; }
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept;
+    void* get() const { return ptr_; }
+    template <typename T> T* as() const { return static_cast<T*>(ptr_); }
+    size_t bytes() const { return bytes_; }
+private:
+    void* ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// Validated configuration with the program-preamble constants resolved
+// (src/Solver/Solver.cpp:260-315, src/HydroGPUApp.cpp:164-226).
+struct ResolvedConfig {
+    hgpu_config cfg;
+    int dim = 0;
+    int numStates = 0;
+    double dx[3] = {1, 1, 1};   // as baked (6 significant digits in REF mode)
+    double gamma = 1.4;         // as baked (%.14g in REF mode)
+    Grid grid;
+};
+ResolvedConfig resolveConfig(const hgpu_config& cfg);
+
+// ---------------- Equation (src/Equation/Equation.cpp, Euler.cpp) ----------------
+class Equation {
+public:
+    virtual ~Equation() = default;
+    std::vector<std::string> states;
+    std::vector<std::string> boundaryMethods;
+    virtual std::string name() const = 0;
+    // kernel chosen for (axis, state, min/max): 0 periodic, 1 mirror, 2 reflect, 3 freeflow, -1 none
+    virtual int stateGetBoundaryKernelForBoundaryMethod(int dim, int state, int minmax) const = 0;
+};
+
+class Euler : public Equation {
+public:
+    Euler(const hgpu_config& cfg, int dim);
+    std::string name() const override { return "Euler"; }
+    int stateGetBoundaryKernelForBoundaryMethod(int dim, int state, int minmax) const override;
+private:
+    hgpu_config cfg_;
+};
+
+template <typename real> class Solver;
+
+// ---------------- Integrator (include/HydroGPU/Integrator/Integrator.h:13-17) ----------------
+template <typename real>
+class Integrator {
+public:
+    explicit Integrator(Solver<real>* s) : solver(s) {}
+    virtual ~Integrator() = default;
+    // computeFlux(stage) must leave the interface fluxes of `stage` in the solver's flux buffer
+    virtual void integrate(const std::function<void(real* stage)>& computeFlux) = 0;
+    // the self-gravity pass with a zero potential (SelfGravitation::applyPotential)
+    virtual void integrateZeroDeriv() = 0;
+    virtual int order() const = 0;
+    virtual int extraBuffers() const = 0;
+protected:
+    Solver<real>* solver;
+};
+
+template <typename real>
+class ForwardEuler : public Integrator<real> {        // src/Integrator/ForwardEuler.cpp
+public:
+    using Integrator<real>::Integrator;
+    void integrate(const std::function<void(real* stage)>& computeFlux) override;
+    void integrateZeroDeriv() override;
+    int order() const override { return 1; }
+    int extraBuffers() const override { return 0; }
+};
+
+template <typename real>
+class RungeKutta : public Integrator<real> {          // include/HydroGPU/Integrator/RungeKutta.h
+public:
+    RungeKutta(Solver<real>* s, int tableau);
+    void integrate(const std::function<void(real* stage)>& computeFlux) override;
+    void integrateZeroDeriv() override;
+    int order() const override { return order_; }
+    int extraBuffers() const override { return nslots_; }
+private:
+    int tableau_, order_, nslots_ = 0;
+    bool alphaIsBinary_ = true;
+    std::vector<CombinePlan<real>> plans_;   // one per stage
+    std::vector<int> inputSlot_;             // stage k reads u^(k) from this slot
+    std::vector<DeviceBuffer> work_;
+    void buildPlans();
+};
+
+// ---------------- Solver (include/HydroGPU/Solver/Solver.h, ISolver.h) ----------------
+class ISolver {
+public:
+    virtual ~ISolver() = default;
+    virtual void init() = 0;
+    virtual void resetState(const void* host, size_t count) = 0;
+    virtual std::string name() const = 0;
+    virtual const Equation& getEquation() const = 0;
+};
+
+// per-launch event pair recorded while profiling (hgpu_profile_update)
+struct LaunchRecord {
+    const char* kind;
+    cudaEvent_t start, stop;
+};
+
+class SolverBase : public ISolver {
+public:
+    virtual ~SolverBase();
+    // launch wrapper: counts kernels and, while profiling, brackets them with events
+    template <class F>
+    void launch(const char* kind, int nkernels, F&& f) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (profiling) { a = eventFromPool(); cudaEventRecord(a, stream); }
+        f();
+        launches_ += nkernels;
+        if (profiling) { b = eventFromPool(); cudaEventRecord(b, stream); records.push_back({kind, a, b}); }
+    }
+    bool profiling = false;
+    std::vector<LaunchRecord> records;
+    std::vector<cudaEvent_t> eventPool;
+    size_t eventNext = 0;
+    cudaEvent_t eventFromPool();
+    int launches_ = 0;                     // kernels launched by the last update()
+    virtual void update() = 0;
+    virtual void readState(void* host, size_t count) = 0;
+    virtual double lastDt() = 0;
+    virtual void* stateDevicePtr() = 0;
+    virtual int kernelsPerStep() const = 0;
+    virtual size_t volume() const = 0;
+    virtual int dim() const = 0;
+    virtual int numStates() const = 0;
+    cudaStream_t stream = nullptr;
+    unsigned* health = nullptr;       // device word
+};
+
+template <typename real>
+class Solver : public SolverBase {
+public:
+    explicit Solver(const ResolvedConfig& rc);
+    ~Solver() override;
+    void init() override;
+    void resetState(const void* host, size_t count) override;
+    void readState(void* host, size_t count) override;
+    const Equation& getEquation() const override { return *equation; }
+    void update() override;                 // Solver::update (Solver.cpp:521-546)
+    void boundary();                        // Solver::boundary (Solver.cpp:448-464)
+    void boundaryOn(real* buf);
+    double lastDt() override;
+    void* stateDevicePtr() override { return state.get(); }
+    size_t volume() const override { return (size_t)rc.grid.V; }
+    int dim() const override { return rc.dim; }
+    int numStates() const override { return rc.numStates; }
+    int kernelsPerStep() const override { return this->launches_; }
+
+    // accessors used by integrators
+    ResolvedConfig rc;
+    Phys<real> ph;
+    DeviceBuffer state, flux, stepConst, dtAcc, healthBuf;
+    std::unique_ptr<Equation> equation;
+    std::unique_ptr<Integrator<real>> integrator;
+    StepConst<real>* sc() const { return stepConst.as<StepConst<real>>(); }
+    unsigned long long accInit() const;
+    int methods[3][2];
+
+protected:
+    virtual void initBuffers();
+    virtual void initStep() {}
+    virtual void calcTimestep() = 0;        // device-side; leaves the minimum in dtAcc
+    virtual void step() = 0;
+    void finalizeDt(bool fixed);
+    void applyPotential();                  // SelfGravitation::applyPotential with a zero potential
+};
+
+template <typename real>
+class FiniteVolumeSolver : public Solver<real> {   // src/Solver/FiniteVolumeSolver.cpp
+public:
+    using Solver<real>::Solver;
+protected:
+    void initBuffers() override;
+};
+
+template <typename real>
+class Roe : public FiniteVolumeSolver<real> {      // src/Solver/Roe.cpp
+public:
+    using FiniteVolumeSolver<real>::FiniteVolumeSolver;
+protected:
+    DeviceBuffer basis, deltaQTilde;
+    void initBuffers() override;
+    void initFlux();                              // calcEigenBasis once per step
+    void calcTimestep() override;
+    void step() override;
+    void calcFlux(real* stage);                   // calcDeltaQTilde + calcFlux
+};
+
+template <typename real>
+class EulerRoe : public Roe<real> {               // src/Solver/EulerRoe.cpp
+public:
+    using Roe<real>::Roe;
+    std::string name() const override { return "EulerRoe"; }
+protected:
+    void step() override;
+};
+
+template <typename real>
+class HLL : public FiniteVolumeSolver<real> {     // src/Solver/HLL.cpp
+public:
+    using FiniteVolumeSolver<real>::FiniteVolumeSolver;
+protected:
+    DeviceBuffer waves;
+    void initBuffers() override;
+    void initStep() override;                     // calcEigenvalues (frozen for the step)
+    void calcTimestep() override;
+    void step() override;
+};
+
+template <typename real>
+class EulerHLL : public HLL<real> {               // src/Solver/EulerHLL.cpp
+public:
+    using HLL<real>::HLL;
+    std::string name() const override { return "EulerHLL"; }
+protected:
+    void step() override;
+};
+
+template <typename real>
+class EulerHLLC : public EulerHLL<real> {         // src/Solver/EulerHLLC.cpp
+public:
+    using EulerHLL<real>::EulerHLL;
+    std::string name() const override { return "EulerHLLC"; }
+};
+
+std::unique_ptr<SolverBase> createSolver(const hgpu_config& cfg);
+
+}  // namespace hgpu

@@ -1,0 +1,127 @@
+// common.cuh -- device-side building blocks shared by the Euler kernels (sm_103a).
+//
+// Arithmetic conventions (parity with the reference OpenCL kernels):
+//  * the .cu files are compiled with --fmad=false, so a*b+c is two roundings as in
+//    the reference source; deliberate fused operations call fma() explicitly;
+//  * a dot/matrix product `sum = 0; sum += M[i][j]*x[j]` (res/RoeEigenfieldLinear.cl:16-54)
+//    is evaluated with its structurally-zero and unit coefficients skipped.  For
+//    finite inputs this is exact: the running sum starts as +0 + first term (which
+//    turns -0 into +0, see zfix) and a running sum started from +0 is never -0, so
+//    adding +/-0 or multiplying by exactly 1 never changes it.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hgpu {
+
+// ---- grid geometry (reference layout: INDEX(x,y,z) = x + SX*(y + SY*z)) ----
+struct Grid {
+    int S[3];            // cells per axis incl. 2 ghost layers per side (1 = unused axis)
+    int dim;
+    long long step[3];   // cell stride per axis
+    long long V;         // S[0]*S[1]*S[2]
+};
+
+__host__ __device__ inline void cellCoords(const Grid& g, long long c, int& x, int& y, int& z) {
+    x = (int)(c % g.S[0]);
+    long long r = c / g.S[0];
+    y = (int)(r % g.S[1]);
+    z = (int)(r / g.S[1]);
+}
+
+// every active coordinate in [lo, S-hi)
+__host__ __device__ inline bool inRange(const Grid& g, int x, int y, int z, int lo, int hi) {
+    if (x < lo || x >= g.S[0] - hi) return false;
+    if (g.dim > 1 && (y < lo || y >= g.S[1] - hi)) return false;
+    if (g.dim > 2 && (z < lo || z >= g.S[2] - hi)) return false;
+    return true;
+}
+
+// face (side, c) is "along" coordinate lo..S-hiA along `side`, transverse lo..S-hiT
+__host__ __device__ inline bool faceInRange(const Grid& g, int side, int x, int y, int z, int hiAlong, int hiTrans) {
+    int c[3] = {x, y, z};
+    for (int a = 0; a < g.dim; ++a) {
+        int hi = (a == side) ? hiAlong : hiTrans;
+        if (c[a] < 2 || c[a] >= g.S[a] - hi) return false;
+    }
+    return true;
+}
+
+// ---- -0 -> +0 (the effect of `+0 + x` in round-to-nearest), integer ops only ----
+__device__ __forceinline__ double zfix(double x) {
+    long long b = __double_as_longlong(x);
+    return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+__device__ __forceinline__ float zfix(float x) {
+    int b = __float_as_int(x);
+    return __int_as_float(b == (int)0x80000000u ? 0 : b);
+}
+
+// ---- finiteness by exponent bits (integer pipe) ----
+__device__ __forceinline__ bool finiteBits(double x) {
+    return (__double_as_longlong(x) & 0x7FF0000000000000LL) != 0x7FF0000000000000LL;
+}
+__device__ __forceinline__ bool finiteBits(float x) { return (__float_as_int(x) & 0x7F800000) != 0x7F800000; }
+template <typename real, int N>
+__device__ __forceinline__ bool allFinite(const real* v) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < N; ++i) ok &= finiteBits(v[i]);
+    return ok;
+}
+
+// ---- ordered-bit atomic minimum of non-negative reals (NaN ignored by construction) ----
+__device__ __forceinline__ unsigned long long realBits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ unsigned long long realBits(float x) { return (unsigned long long)(unsigned int)__float_as_int(x); }
+__host__ __device__ inline double bitsToDouble(unsigned long long b, bool isFloat) {
+#ifdef __CUDA_ARCH__
+    return isFloat ? (double)__int_as_float((int)(unsigned int)b) : __longlong_as_double((long long)b);
+#else
+    if (isFloat) { unsigned int u = (unsigned int)b; float f; memcpy(&f, &u, 4); return f; }
+    double d; memcpy(&d, &b, 8); return d;
+#endif
+}
+
+// ---- health word bits (hgpu_health) ----
+enum : unsigned int { HEALTH_NONFINITE_DT = 1u, HEALTH_HLLC_NOBRANCH = 2u };
+
+// ---- slope limiters: res/SlopeLimiter.cl:5-68, min/max with fmin/fmax semantics ----
+// `real` is the program type; literals written `2.` in the reference are double, so the
+// FP64 instantiation is exact and the FP32 one follows the same expressions in float.
+template <typename real>
+__device__ __forceinline__ real slopeLimiter(int lim, real r) {
+    switch (lim) {
+    case 0: return (real)0.;                                                         // DonorCell
+    case 1: return (real)1.;                                                         // LaxWendroff
+    case 2: return r;                                                                // BeamWarming
+    case 3: return (real).5 * ((real)1. + r);                                        // Fromm
+    case 4: return fmax((real)0., r) * ((real)3. * r + (real)1.) / ((r + (real)1.) * (r + (real)1.));  // CHARM
+    case 5: return fmax((real)0., (real)1.5 * (r + fabs(r)) / (r + (real)2.));      // HCUS
+    case 6: return fmax((real)0., (real)2. * (r + fabs(r)) / (r + (real)3.));       // HQUICK
+    case 7: return fmax((real)0., fmin((real)2. * r, fmin(((real)1. + (real)2. * r) / (real)3., (real)2.)));  // Koren
+    case 8: return fmax((real)0., fmin(r, (real)1.));                                // MinMod
+    case 9: return fmax((real)0., fmin(r, (real)1.5));                               // Oshker
+    case 10: return (real).5 * (r * r + r) / (r * r + r + (real)1.);                 // Ospre
+    case 11: return fmax((real)0., fmin((real)2. * r, fmin((real).25 + (real).75 * r, (real)4.)));  // Smart
+    case 12: return fmax((real)0., fmax(fmin((real)1.5 * r, (real)1.), fmin(r, (real)1.5)));       // Sweby
+    case 13: return fmax((real)0., fmin(fmin((real)2. * r, (real).75 + (real).25 * r), fmin((real).25 + (real).75 * r, (real)2.)));  // UMIST
+    case 14: return (r * r + r) / (r * r + (real)1.);                                // VanAlbada1
+    case 15: return (real)2. * r / (r * r + (real)1.);                               // VanAlbada2
+    case 16: return fmax((real)0., r) * (real)2. / ((real)1. + r);                  // VanLeer
+    case 17: return fmax((real)0., fmin((real)2., fmin((real).5 * ((real)1. + r), (real)2. * r)));  // MonotizedCentral
+    case 18: return fmax((real)0., fmax(fmin((real)1., (real)2. * r), fmin((real)2., r)));         // Superbee
+    case 19: return (real).5 * (r + (real)1.) * fmin((real)1., fmin((real)4. * r / (r + (real)1.), (real)4. / (r + (real)1.)));  // BarthJespersen
+    }
+    return (real)0.;
+}
+
+// ---- per-step constants kept on the device (dt never leaves the GPU during a step) ----
+template <typename real>
+struct StepConst {
+    real dt;             // this step's dt (min * cfl, or the fixed dt)
+    real dt_dx[3];       // dt / dx[side]   (res/Roe.cl:206)
+    real coef[4][4];     // beta(m,k) * dt  (RungeKutta.h:86-99, computed in `real`)
+    double dt_f64;       // dt widened, for the host
+};
+
+}  // namespace hgpu

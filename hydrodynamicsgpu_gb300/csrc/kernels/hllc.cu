@@ -1,0 +1,241 @@
+// hllc.cu -- EulerHLLC kernels for sm_103a: wave speeds + CFL timestep once per
+// step, HLLC interface flux once per Runge-Kutta stage.
+//
+// Reference kernels replaced (res/EulerHLLC.cl): calcEigenvalues (:15-131),
+// calcCellTimestep (:135-168), calcFlux with HLLC_METHOD 2 (:170-445).  Only the
+// outer wave speeds sl and sr are kept per face: the middle eigenvalues (the Roe
+// velocity) are never read by the timestep or the flux.  The reference's slope
+// limiter for HLLC is compiled out (:393-411), so the flux is first order.
+// A face where no HLLC branch applies keeps the flux of its previous evaluation,
+// momentum components swapped back once more, exactly as the reference buffer does.
+#include "kernels.h"
+#include "reduce.cuh"
+
+namespace hgpu {
+namespace {
+
+constexpr int kThreads = 256;
+inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// state rotated so the normal momentum is component 1 (EulerHLLC.cl:32-47)
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void loadRotated(const real* __restrict__ s, long long c, real* out) {
+#pragma unroll
+    for (int j = 0; j < D + 2; ++j) out[j] = s[(long long)(D + 2) * c + j];
+    if (SIDE > 0) { real t = out[1]; out[1] = out[1 + SIDE]; out[1 + SIDE] = t; }
+}
+
+template <typename real, int D>
+struct Prim {
+    real density, invDensity, v[3], velocitySq, energyTotal, pressure, enthalpyTotal;
+};
+
+// primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238), potential 0
+template <typename real, int D>
+__device__ __forceinline__ void primitives(const real* st, real gm1, Prim<real, D>& p) {
+    const int E = D + 1;
+    p.density = st[0];
+    p.invDensity = (real)1. / p.density;
+#pragma unroll
+    for (int k = 0; k < D; ++k) p.v[k] = st[1 + k] / p.density;
+    p.velocitySq = p.v[0] * p.v[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + p.v[k] * p.v[k];
+    p.energyTotal = st[E] * p.invDensity;
+    real energyKinetic = (real).5f * p.velocitySq;
+    real energyInternal = p.energyTotal - energyKinetic;
+    p.pressure = gm1 * p.density * energyInternal;
+    p.enthalpyTotal = p.energyTotal + p.pressure * p.invDensity;
+}
+
+// sl, sr of one face (EulerHLLC.cl:85-97)
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, real gq, const real* __restrict__ state,
+                                         real* __restrict__ waves, long long c) {
+    real sL[D + 2], sR[D + 2];
+    loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
+    loadRotated<real, D, SIDE>(state, c, sR);
+    const real gm1 = ph.gamma - (real)1.;
+    Prim<real, D> L, R;
+    primitives<real, D>(sL, gm1, L);
+    primitives<real, D>(sR, gm1, R);
+    real cL = sqrt(gm1 * (L.enthalpyTotal - (real).5f * L.velocitySq));
+    real cR = sqrt(gm1 * (R.enthalpyTotal - (real).5f * R.velocitySq));
+    real pressureStar = fmax((real)0., (real).5f * (L.pressure + R.pressure) -
+                                           (real).5f * (R.v[0] - L.v[0]) * (real).5f * (L.density + R.density) *
+                                               (real).5f * (cL + cR));
+    real qL = pressureStar <= L.pressure ? (real)1. : sqrt((real)1. + gq * (pressureStar / L.pressure - (real)1.));
+    real qR = pressureStar <= R.pressure ? (real)1. : sqrt((real)1. + gq * (pressureStar / R.pressure - (real)1.));
+    waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - cL * qL;
+    waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + cR * qR;
+}
+
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) hllcWaveKernel(Grid g, Phys<real> ph, real gq,
+                                                           const real* __restrict__ state, real* __restrict__ waves) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    if (!inRange(g, x, y, z, 2, 1)) return;    // every axis in [2, S-2] (EulerHLLC.cl:115-123)
+    waveFace<real, D, 0>(g, ph, gq, state, waves, c);
+    if (D > 1) waveFace<real, D, (D > 1 ? 1 : 0)>(g, ph, gq, state, waves, c);
+    if (D > 2) waveFace<real, D, (D > 2 ? 2 : 0)>(g, ph, gq, state, waves, c);
+}
+
+// cells in [2, S-2]: min over sides of dx / (max(0, sr(face c)) - min(0, sl(face c+1)))
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) hllcDtKernel(Grid g, Phys<real> ph, const real* __restrict__ waves,
+                                                         unsigned long long* acc, unsigned* health) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long best = ~0ULL;
+    bool nan = false;
+    if (c < g.V) {
+        int x, y, z;
+        cellCoords(g, c, x, y, z);
+        real result = (real)INFINITY;
+        if (inRange(g, x, y, z, 2, 1)) {
+#pragma unroll
+            for (int side = 0; side < D; ++side) {
+                real srHere = waves[((long long)side * 2 + 1) * g.V + c];
+                real slNext = waves[((long long)side * 2 + 0) * g.V + c + g.step[side]];
+                real minLambda = (real)fmin(0., (double)slNext);
+                real maxLambda = (real)fmax(0., (double)srHere);
+                real dum = ph.dx[side] / (maxLambda - minLambda);
+                if (dum != dum) nan = true;
+                result = fmin(result, dum);
+            }
+        }
+        best = realBits(result);
+    }
+    if (nan) atomicOr(health, HEALTH_NONFINITE_DT);
+    blockMinToGlobal(best, acc);
+}
+
+// HLLC flux, HLLC_METHOD 2 (EulerHLLC.cl:240-418); `flux` holds the face's previous value.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
+                                         const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c) {
+    const int N = D + 2, E = N - 1;
+    real stL[N], stR[N];
+    loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
+    loadRotated<real, D, SIDE>(stage, c, stR);
+    const real gm1 = ph.gamma - (real)1.;
+    Prim<real, D> L, R;
+    primitives<real, D>(stL, gm1, L);
+    primitives<real, D>(stR, gm1, R);
+    real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
+    real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
+    real fL[N], fR[N], flux[N];
+    fL[0] = L.density * L.v[0];
+    fL[1] = L.density * L.v[0] * L.v[0] + L.pressure;
+#pragma unroll
+    for (int k = 1; k < D; ++k) fL[1 + k] = L.density * L.v[k] * L.v[0];
+    fL[E] = L.density * L.enthalpyTotal * L.v[0];
+    fR[0] = R.density * R.v[0];
+    fR[1] = R.density * R.v[0] * R.v[0] + R.pressure;
+#pragma unroll
+    for (int k = 1; k < D; ++k) fR[1 + k] = R.density * R.v[k] * R.v[0];
+    fR[E] = R.density * R.enthalpyTotal * R.v[0];
+    real sStar = (R.density * R.v[0] * (sr - R.v[0]) - L.density * L.v[0] * (sl - L.v[0]) + L.pressure - R.pressure) /
+                 (R.density * (sr - R.v[0]) - L.density * (sl - L.v[0]));
+    bool taken = true;
+    if ((real)0. <= sl) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[i] = fL[i];
+    } else if (sl <= (real)0. && (real)0. <= sStar) {
+        real pressureLR = (real).5f * (L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
+                                       R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        flux[0] = sStar * (sl * stL[0] - fL[0]) / (sl - sStar);
+        flux[1] = (sStar * (sl * stL[1] - fL[1]) + sl * pressureLR) / (sl - sStar);
+#pragma unroll
+        for (int k = 1; k < D; ++k) flux[1 + k] = sStar * (sl * stL[1 + k] - fL[1 + k]) / (sl - sStar);
+        flux[E] = (sStar * (sl * stL[E] - fL[E]) + sl * pressureLR * sStar) / (sl - sStar);
+    } else if (sStar <= (real)0. && (real)0. <= sr) {
+        real pressureLR = (real).5f * (L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
+                                       R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        flux[0] = sStar * (sr * stR[0] - fR[0]) / (sr - sStar);
+        flux[1] = (sStar * (sr * stR[1] - fR[1]) + sr * pressureLR) / (sr - sStar);
+#pragma unroll
+        for (int k = 1; k < D; ++k) flux[1 + k] = sStar * (sr * stR[1 + k] - fR[1 + k]) / (sr - sStar);
+        flux[E] = (sStar * (sr * stR[E] - fR[E]) + sr * pressureLR * sStar) / (sr - sStar);
+    } else if (sr <= (real)0.) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[i] = fR[i];
+    } else {
+        // no branch: the reference leaves the buffer's previous (global-frame) value,
+        // then applies the rotate-back swap to it
+        taken = false;
+#pragma unroll
+        for (int j = 0; j < N; ++j) flux[j] = fluxBuf[((long long)SIDE * N + j) * g.V + c];
+    }
+    if (SIDE > 0) { real t = flux[1]; flux[1] = flux[1 + SIDE]; flux[1 + SIDE] = t; }
+#pragma unroll
+    for (int j = 0; j < N; ++j) fluxBuf[((long long)SIDE * N + j) * g.V + c] = flux[j];
+    return taken;
+}
+
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph, const real* __restrict__ stage,
+                                                           const real* __restrict__ waves, real* __restrict__ flux,
+                                                           unsigned* health) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    bool ok = true;
+    int cc[3] = {x, y, z};
+    // faces along `side` in [2, S-2], transverse interior [2, S-3] (the ones calcFluxDeriv reads)
+#pragma unroll
+    for (int side = 0; side < D; ++side) {
+        bool in = true;
+        for (int a = 0; a < D; ++a) {
+            int hi = a == side ? 1 : 2;
+            if (cc[a] < 2 || cc[a] >= g.S[a] - hi) in = false;
+        }
+        if (!in) continue;
+        if (side == 0) ok &= hllcFace<real, D, 0>(g, ph, stage, waves, flux, c);
+        else if (side == 1) ok &= hllcFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
+        else ok &= hllcFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+    }
+    if (!ok) atomicOr(health, HEALTH_HLLC_NOBRANCH);
+}
+
+}  // namespace
+
+template <typename real>
+void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, cudaStream_t st) {
+    // (gamma + 1.) / (2. * gamma) is a per-program constant; computed once, identically
+    real gq = (ph.gamma + (real)1.) / ((real)2. * ph.gamma);
+    if (g.dim == 1) hllcWaveKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
+    else if (g.dim == 2) hllcWaveKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
+    else hllcWaveKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
+}
+
+template <typename real>
+void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsigned long long* acc, unsigned* health,
+                  cudaStream_t st) {
+    if (g.dim == 1) hllcDtKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, waves, acc, health);
+    else if (g.dim == 2) hllcDtKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, waves, acc, health);
+    else hllcDtKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, waves, acc, health);
+}
+
+template <typename real>
+void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
+                    unsigned* health, cudaStream_t st) {
+    if (g.dim == 1) hllcFluxKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health);
+    else if (g.dim == 2) hllcFluxKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health);
+    else hllcFluxKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health);
+}
+
+#define INST(real)                                                                                                \
+    template void launchHllcWaves<real>(const Grid&, const Phys<real>&, const real*, real*, cudaStream_t);        \
+    template void launchHllcDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
+                                     cudaStream_t);                                                               \
+    template void launchHllcFlux<real>(const Grid&, const Phys<real>&, const real*, const real*, real*, unsigned*, \
+                                       cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace hgpu

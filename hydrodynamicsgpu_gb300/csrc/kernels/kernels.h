@@ -1,0 +1,81 @@
+// kernels.h -- host-side launchers of the sm_103a Euler kernels (plain C++ types).
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace hgpu {
+
+template <typename real>
+struct Phys {
+    real dx[3];      // DX/DY/DZ as the program bakes them
+    real gamma;      // ((real)<defs value>)
+    float cfl;
+};
+
+// One output row of the Runge-Kutta combine at a stage (see combine.cu).
+template <typename real>
+struct CombineOp {
+    int out;         // slot written
+    int prior;       // slot holding the partial sum so far, or -1 (sum starts at +0)
+    int priorAlias;  // the prior is u^n itself (sum == +0 + u^n): read it through zfix
+    int hasAlpha;    // add alpha * u^(k)
+    int alphaIsOne;
+    real alpha;
+    int hasBeta;     // add (beta * dt) * d^(k), coefficient from StepConst::coef[brow][bcol]
+    int brow, bcol;
+};
+
+template <typename real>
+struct CombinePlan {
+    int fe;                   // forward Euler: slot[0] = slot[0] + d * dt
+    int in;                   // slot of the stage input u^(k)
+    int nops;
+    CombineOp<real> ops[4];
+    real* slot[8];
+};
+
+// ---- boundary.cu ----
+template <typename real>
+void launchBoundary(const Grid& g, const int methods[3][2], real* state, cudaStream_t st);
+template <typename real>
+void launchDerivCombine(const Grid& g, const Phys<real>& ph, const real* flux, const CombinePlan<real>& plan,
+                        const StepConst<real>* sc, cudaStream_t st);
+template <typename real>
+void launchAlphaOnly(const Grid& g, int integrator, real* state, const StepConst<real>* sc, cudaStream_t st);
+template <typename real>
+void launchZeroAdd(const Grid& g, real* state, const StepConst<real>* sc, cudaStream_t st);
+template <typename real>
+void launchFinalizeDt(const Phys<real>& ph, int integrator, int useFixed, double fixedDt, unsigned long long* acc,
+                      unsigned long long accInit, StepConst<real>* sc, unsigned* health, cudaStream_t st);
+template <typename real>
+void launchResetAcc(unsigned long long* acc, unsigned long long accInit, cudaStream_t st);
+
+// ---- roe.cu ----
+template <typename real>
+void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st);
+template <typename real>
+void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigned long long* acc, unsigned* health,
+                 cudaStream_t st);
+template <typename real>
+void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* dq, int seam, cudaStream_t st);
+template <typename real>
+void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
+                   const StepConst<real>* sc, real* flux, int seam, cudaStream_t st);
+int roeRecordSize(int dim);
+
+// ---- hllc.cu ----
+template <typename real>
+void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, cudaStream_t st);
+template <typename real>
+void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsigned long long* acc, unsigned* health,
+                  cudaStream_t st);
+template <typename real>
+void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
+                    unsigned* health, cudaStream_t st);
+
+// ---- tableaus (combine.cu): alpha/beta in double, order ----
+int tableauOrder(int integrator);
+double tableauAlpha(int integrator, int m, int k);
+double tableauBeta(int integrator, int m, int k);
+
+}  // namespace hgpu

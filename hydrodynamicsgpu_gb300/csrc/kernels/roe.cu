@@ -1,0 +1,217 @@
+// roe.cu -- EulerRoe kernels for sm_103a: eigenbasis + CFL timestep once per step,
+// Delta-q-tilde and limited flux once per Runge-Kutta stage.
+//
+// Reference kernels replaced: calcEigenBasis (res/EulerRoe.cl:261-271),
+// calcCellTimestep (res/Roe.cl:4-65), calcDeltaQTilde (res/Roe.cl:152-168),
+// calcFlux (res/Roe.cl:301-320).  The eigenbasis is stored as a compact record of
+// RoeRec<D>::NB distinct entries per face (structure-of-arrays, one plane per
+// entry) instead of two dense N x N matrices, and it is computed once per step
+// from u^n exactly as the reference does (Roe.cpp:82-92).
+#include "kernels.h"
+#include "roe.cuh"
+#include "reduce.cuh"
+
+namespace hgpu {
+
+int roeRecordSize(int dim) {
+    return dim == 1 ? RoeRec<1>::NB : dim == 2 ? RoeRec<2>::NB : RoeRec<3>::NB;
+}
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// faces along `side` in [loA, S-hiA), transverse in [2, S-2-1]
+__device__ __forceinline__ bool roeFace(const Grid& g, int side, int x, int y, int z, int loA, int hiA) {
+    int c[3] = {x, y, z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a >= g.dim) break;
+        int lo = a == side ? loA : 2, hi = a == side ? hiA : 2;
+        if (c[a] < lo || c[a] >= g.S[a] - hi) return false;
+    }
+    return true;
+}
+
+template <typename real, int D>
+__device__ __forceinline__ void loadState(const real* __restrict__ s, long long c, real* out) {
+#pragma unroll
+    for (int j = 0; j < D + 2; ++j) out[j] = s[(long long)(D + 2) * c + j];
+}
+
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void basisFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ state,
+                                          real* __restrict__ basis, long long c, const real* sR) {
+    const int N = D + 2, NB = RoeRec<D>::NB;
+    real sL[N], rec[NB];
+    loadState<real, D>(state, c - g.step[SIDE], sL);
+    roeBasis<real, D, SIDE>(sL, sR, ph.gamma, rec);
+#pragma unroll
+    for (int k = 0; k < NB; ++k) basis[((long long)SIDE * NB + k) * g.V + c] = rec[k];
+}
+
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) roeBasisKernel(Grid g, Phys<real> ph, const real* __restrict__ state,
+                                                           real* __restrict__ basis, int loA, int hiA) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    real sR[D + 2];
+    loadState<real, D>(state, c, sR);
+    if (roeFace(g, 0, x, y, z, loA, hiA)) basisFace<real, D, 0>(g, ph, state, basis, c, sR);
+    if (D > 1 && roeFace(g, 1, x, y, z, loA, hiA)) basisFace<real, D, (D > 1 ? 1 : 0)>(g, ph, state, basis, c, sR);
+    if (D > 2 && roeFace(g, 2, x, y, z, loA, hiA)) basisFace<real, D, (D > 2 ? 2 : 0)>(g, ph, state, basis, c, sR);
+}
+
+// per interior cell and side: dx / (|max(0, lambda_max(face c)) - min(0, lambda_min(face c+1))| + 1e-9)
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) roeDtKernel(Grid g, Phys<real> ph, const real* __restrict__ basis,
+                                                        unsigned long long* acc, unsigned* health) {
+    typedef RoeRec<D> R_;
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long best = ~0ULL;
+    bool nan = false;
+    if (c < g.V) {
+        int x, y, z;
+        cellCoords(g, c, x, y, z);
+        if (inRange(g, x, y, z, 2, 2)) {
+#pragma unroll
+            for (int side = 0; side < D; ++side) {
+                real lamMax = basis[((long long)side * R_::NB + R_::LAME) * g.V + c];
+                real lamMin = basis[((long long)side * R_::NB + R_::LAM0) * g.V + c + g.step[side]];
+                real maxLambda = fmax((real)0., lamMax);
+                real minLambda = fmin((real)0., lamMin);
+                real dum = (real)((double)ph.dx[side] / ((double)fabs(maxLambda - minLambda) + 1e-9));
+                if (dum != dum) nan = true;
+                unsigned long long b = realBits(dum);
+                best = b < best ? b : best;
+            }
+        } else if (c < g.V) {
+            best = realBits((real)INFINITY);
+        }
+    }
+    if (nan) atomicOr(health, HEALTH_NONFINITE_DT);
+    blockMinToGlobal(best, acc);
+}
+
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void deltaQFace(const Grid& g, const real* __restrict__ stage, const real* __restrict__ basis,
+                                           real* __restrict__ dq, long long c, const real* sR) {
+    const int N = D + 2, NB = RoeRec<D>::NB;
+    real sL[N], rec[NB], ds[N], y[N];
+    loadState<real, D>(stage, c - g.step[SIDE], sL);
+#pragma unroll
+    for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)SIDE * NB + k) * g.V + c];
+#pragma unroll
+    for (int j = 0; j < N; ++j) ds[j] = sR[j] - sL[j];
+    leftTransform<real, D, SIDE>(rec, ds, y);
+#pragma unroll
+    for (int i = 0; i < N; ++i) dq[((long long)SIDE * N + i) * g.V + c] = y[i];
+}
+
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) roeDeltaQKernel(Grid g, const real* __restrict__ stage,
+                                                            const real* __restrict__ basis, real* __restrict__ dq,
+                                                            int loA, int hiA) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    real sR[D + 2];
+    loadState<real, D>(stage, c, sR);
+    if (roeFace(g, 0, x, y, z, loA, hiA)) deltaQFace<real, D, 0>(g, stage, basis, dq, c, sR);
+    if (D > 1 && roeFace(g, 1, x, y, z, loA, hiA)) deltaQFace<real, D, (D > 1 ? 1 : 0)>(g, stage, basis, dq, c, sR);
+    if (D > 2 && roeFace(g, 2, x, y, z, loA, hiA)) deltaQFace<real, D, (D > 2 ? 2 : 0)>(g, stage, basis, dq, c, sR);
+}
+
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void fluxFace(const Grid& g, int lim, real dt_dx, const real* __restrict__ stage,
+                                         const real* __restrict__ basis, const real* __restrict__ dq,
+                                         real* __restrict__ flux, long long c, const real* sR) {
+    const int N = D + 2, NB = RoeRec<D>::NB;
+    real sL[N], rec[NB], qL[N], q[N], qR[N], F[N];
+    const long long st = g.step[SIDE];
+    loadState<real, D>(stage, c - st, sL);
+#pragma unroll
+    for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)SIDE * NB + k) * g.V + c];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const real* p = dq + ((long long)SIDE * N + i) * g.V + c;
+        qL[i] = p[-st];
+        q[i] = p[0];
+        qR[i] = p[st];
+    }
+    roeFlux<real, D, SIDE>(rec, sL, sR, qL, q, qR, dt_dx, lim, F);
+#pragma unroll
+    for (int j = 0; j < N; ++j) flux[((long long)SIDE * N + j) * g.V + c] = F[j];
+}
+
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) roeFluxKernel(Grid g, int lim, const real* __restrict__ stage,
+                                                          const real* __restrict__ basis, const real* __restrict__ dq,
+                                                          const StepConst<real>* __restrict__ sc,
+                                                          real* __restrict__ flux) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    real sR[D + 2];
+    loadState<real, D>(stage, c, sR);
+    if (roeFace(g, 0, x, y, z, 2, 1)) fluxFace<real, D, 0>(g, lim, sc->dt_dx[0], stage, basis, dq, flux, c, sR);
+    if (D > 1 && roeFace(g, 1, x, y, z, 2, 1))
+        fluxFace<real, D, (D > 1 ? 1 : 0)>(g, lim, sc->dt_dx[1], stage, basis, dq, flux, c, sR);
+    if (D > 2 && roeFace(g, 2, x, y, z, 2, 1))
+        fluxFace<real, D, (D > 2 ? 2 : 0)>(g, lim, sc->dt_dx[2], stage, basis, dq, flux, c, sR);
+}
+
+}  // namespace
+
+// REF: faces along [2, S-2] (res/EulerRoe.cl:27-34, res/Roe.cl:88-95); SEAM: [1, S-1].
+template <typename real>
+void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st) {
+    int loA = seam ? 1 : 2, hiA = seam ? 0 : 1;
+    if (g.dim == 1) roeBasisKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, state, basis, loA, hiA);
+    else if (g.dim == 2) roeBasisKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, state, basis, loA, hiA);
+    else roeBasisKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, state, basis, loA, hiA);
+}
+
+template <typename real>
+void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigned long long* acc, unsigned* health,
+                 cudaStream_t st) {
+    if (g.dim == 1) roeDtKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, basis, acc, health);
+    else if (g.dim == 2) roeDtKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, basis, acc, health);
+    else roeDtKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, basis, acc, health);
+}
+
+template <typename real>
+void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* dq, int seam, cudaStream_t st) {
+    int loA = seam ? 1 : 2, hiA = seam ? 0 : 1;
+    if (g.dim == 1) roeDeltaQKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
+    else if (g.dim == 2) roeDeltaQKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
+    else roeDeltaQKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
+}
+
+template <typename real>
+void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
+                   const StepConst<real>* sc, real* flux, int seam, cudaStream_t st) {
+    (void)seam;
+    if (g.dim == 1) roeFluxKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+    else if (g.dim == 2) roeFluxKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+    else roeFluxKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+}
+
+#define INST(real)                                                                                              \
+    template void launchRoeBasis<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t);  \
+    template void launchRoeDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
+                                    cudaStream_t);                                                             \
+    template void launchRoeDeltaQ<real>(const Grid&, const real*, const real*, real*, int, cudaStream_t);       \
+    template void launchRoeFlux<real>(const Grid&, int, const real*, const real*, const real*,                   \
+                                      const StepConst<real>*, real*, int, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace hgpu

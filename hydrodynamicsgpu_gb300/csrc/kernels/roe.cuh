@@ -1,0 +1,250 @@
+// roe.cuh -- Roe eigenbasis, characteristic transforms and limited flux (device code).
+//
+// The scheme is HydroGPU's EulerRoe (res/EulerRoe.cl:18-259, res/Roe.cl:4-320,
+// res/RoeEigenfieldLinear.cl:16-74): per interface the Roe-averaged state gives
+// eigenvalues, right eigenvectors R and left eigenvectors L = R^-1, built in the
+// frame whose x axis is the interface normal and rotated back by swapping the
+// momentum-x and momentum-side rows/columns.  Here the basis of a face is kept in
+// its normal frame as a compact record of the distinct matrix entries; the swap is
+// applied as an index permutation when the matrices are used.  Every entry is
+// computed with the reference's expression and operation order, so the values are
+// bit-identical; sums over matrix columns keep the reference's column order in the
+// global frame (see common.cuh for the zero/unit-coefficient rule).
+#pragma once
+#include "common.cuh"
+
+namespace hgpu {
+
+// record layout (per face, normal frame)
+template <int D>
+struct RoeRec {
+    enum {
+        N = D + 2,
+        LAM0 = 0,   // vx - c              (= R[1][0])
+        VX = 1,     // normal Roe velocity
+        LAME = 2,   // vx + c              (= R[1][E])
+        HM = 3,     // H - c*vx            (R[E][0])
+        HV2 = 4,    // .5 * |v|^2          (R[E][1])
+        HP = 5,     // H + c*vx            (R[E][E])
+        VT = 6,     // tangential velocities vt[0..D-2]
+        L0 = 6 + (D - 1),   // left row 0, N entries (normal frame columns)
+        L1 = L0 + N,        // left row 1, N entries
+        LE0 = L1 + N,       // left row E, column 0
+        LE1 = LE0 + 1,      // left row E, column 1 (columns >= 2 equal row 0's)
+        NB = LE1 + 1
+    };
+};
+
+// global component j <-> normal-frame component for interface `side` (swap 1 <-> 1+side)
+template <int SIDE>
+__device__ __forceinline__ constexpr int perm(int j) { return j == 1 ? 1 + SIDE : (j == 1 + SIDE ? 1 : j); }
+
+// Eigen basis of one interface (res/EulerRoe.cl:36-226 with solid == 0, potential == 0).
+// sL, sR: global-frame conserved states of the cells left/right of the face.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void roeBasis(const real* sL, const real* sR, real gamma, real* rec) {
+    typedef RoeRec<D> R_;
+    const int N = D + 2, E = N - 1;
+    const real gm1 = gamma - (real)1.f;
+    real rhoL = sL[0], rhoR = sR[0];
+    // VELOCITY(ptr) = (m..., 0)/rho componentwise (res/include/HydroGPU/Euler.h:6-12)
+    real vL[3], vR[3];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { vL[k] = sL[1 + k] / rhoL; vR[k] = sR[1 + k] / rhoR; }
+    // dot(v,v) over 4 components; the zero components add +0 to a non-negative sum
+    real vvL = vL[0] * vL[0], vvR = vR[0] * vR[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) { vvL = vvL + vL[k] * vL[k]; vvR = vvR + vR[k] * vR[k]; }
+    real invDensityL = (real)1.f / rhoL;
+    real energyTotalL = sL[E] * invDensityL;
+    real energyKineticL = (real).5f * vvL;
+    real energyInternalL = energyTotalL - energyKineticL;        // - potential (0)
+    real pressureL = gm1 * rhoL * energyInternalL;
+    real enthalpyTotalL = energyTotalL + pressureL * invDensityL;
+    real roeWeightL = sqrt(rhoL);
+    real invDensityR = (real)1.f / rhoR;
+    real energyTotalR = sR[E] * invDensityR;
+    real energyKineticR = (real).5f * vvR;
+    real energyInternalR = energyTotalR - energyKineticR;
+    real pressureR = gm1 * rhoR * energyInternalR;
+    real enthalpyTotalR = energyTotalR + pressureR * invDensityR;
+    real roeWeightR = sqrt(rhoR);
+    real norm = (real)1.f / (roeWeightL + roeWeightR);
+    real v[3];
+#pragma unroll
+    for (int k = 0; k < D; ++k) v[k] = (roeWeightL * vL[k] + roeWeightR * vR[k]) * norm;
+    real enthalpyTotal = (roeWeightL * enthalpyTotalL + roeWeightR * enthalpyTotalR) * norm;
+    real velocitySq = v[0] * v[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) velocitySq = velocitySq + v[k] * v[k];
+    real c = sqrt((enthalpyTotal - (real).5f * velocitySq) * gm1);  // - energyPotential (0)
+    // rotate: normal velocity first (res/EulerRoe.cl:101-110)
+    real vx = v[SIDE];
+    real vt[2] = {0, 0};
+    if (D > 1) vt[0] = (SIDE == 1) ? v[0] : v[1];
+    if (D > 2) vt[1] = (SIDE == 2) ? v[0] : v[2];
+    rec[R_::LAM0] = vx - c;
+    rec[R_::VX] = vx;
+    rec[R_::LAME] = vx + c;
+    rec[R_::HM] = enthalpyTotal - c * vx;
+    rec[R_::HV2] = (real).5f * velocitySq;
+    rec[R_::HP] = enthalpyTotal + c * vx;
+#pragma unroll
+    for (int t = 0; t < D - 1; ++t) rec[R_::VT + t] = vt[t];
+    real invDenom = (real).5f / (c * c);
+    real h = (real).5f * gm1;
+    rec[R_::L0 + 0] = (h * velocitySq + c * vx) * invDenom;
+    rec[R_::L0 + 1] = -(c + gm1 * vx) * invDenom;
+#pragma unroll
+    for (int t = 0; t < D - 1; ++t) rec[R_::L0 + 2 + t] = -gm1 * vt[t] * invDenom;
+    rec[R_::L0 + E] = gm1 * invDenom;
+    rec[R_::L1 + 0] = (real)1.f - gm1 * velocitySq * invDenom;
+    rec[R_::L1 + 1] = gm1 * vx * (real)2.f * invDenom;
+#pragma unroll
+    for (int t = 0; t < D - 1; ++t) rec[R_::L1 + 2 + t] = gm1 * vt[t] * (real)2.f * invDenom;
+    rec[R_::L1 + E] = -gm1 * (real)2.f * invDenom;
+    rec[R_::LE0] = (h * velocitySq - c * vx) * invDenom;
+    rec[R_::LE1] = (c - gm1 * vx) * invDenom;
+}
+
+// Normal-frame matrix entries, including the structural zeros and ones.
+template <typename real, int D>
+__device__ __forceinline__ real leftEntry(const real* rec, int i, int c) {
+    typedef RoeRec<D> R_;
+    const int E = D + 1;
+    if (i == 0) return rec[R_::L0 + c];
+    if (i == 1) return rec[R_::L1 + c];
+    if (i == E) return c == 0 ? rec[R_::LE0] : (c == 1 ? rec[R_::LE1] : rec[R_::L0 + c]);
+    return c == 0 ? -rec[R_::VT + i - 2] : (c == i ? (real)1.f : (real)0.f);
+}
+template <typename real, int D>
+__device__ __forceinline__ real rightEntry(const real* rec, int i, int j) {
+    typedef RoeRec<D> R_;
+    const int E = D + 1;
+    if (j == 0 || j == 1 || j == E) {
+        if (i == 0) return (real)1.f;
+        if (i == 1) return j == 0 ? rec[R_::LAM0] : (j == 1 ? rec[R_::VX] : rec[R_::LAME]);
+        if (i == E) return j == 0 ? rec[R_::HM] : (j == 1 ? rec[R_::HV2] : rec[R_::HP]);
+        return rec[R_::VT + i - 2];
+    }
+    if (i == j) return (real)1.f;
+    if (i == E) return rec[R_::VT + j - 2];
+    return (real)0.f;
+}
+
+// Dense forms, term for term as res/RoeEigenfieldLinear.cl:16-54 (used when an input
+// is not finite: then 0 * Inf/NaN terms matter).
+template <typename real, int D, int SIDE>
+__device__ __noinline__ void leftTransformDense(const real* rec, const real* x, real* y) {
+    const int N = D + 2;
+    for (int i = 0; i < N; ++i) {
+        real s = (real)0.f;
+        for (int j = 0; j < N; ++j) s = s + leftEntry<real, D>(rec, i, perm<SIDE>(j)) * x[j];
+        y[i] = s;
+    }
+}
+template <typename real, int D, int SIDE>
+__device__ __noinline__ void rightTransformDense(const real* rec, const real* f, real* F) {
+    const int N = D + 2;
+    for (int g = 0; g < N; ++g) {
+        int i = perm<SIDE>(g);
+        real s = (real)0.f;
+        for (int j = 0; j < N; ++j) s = s + rightEntry<real, D>(rec, i, j) * f[j];
+        F[g] = s;
+    }
+}
+
+// y = L x with L in the global frame: y_i = sum_j L[i][perm(j)] x_j, j ascending.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void leftTransform(const real* rec, const real* x, real* y) {
+    typedef RoeRec<D> R_;
+    const int N = D + 2, E = N - 1;
+    if (!allFinite<real, N>(x)) { leftTransformDense<real, D, SIDE>(rec, x, y); return; }
+    // row 0 and row 1: dense
+    {
+        real s0 = zfix(rec[R_::L0 + perm<SIDE>(0)] * x[0]);
+        real s1 = zfix(rec[R_::L1 + perm<SIDE>(0)] * x[0]);
+#pragma unroll
+        for (int j = 1; j < N; ++j) {
+            s0 = s0 + rec[R_::L0 + perm<SIDE>(j)] * x[j];
+            s1 = s1 + rec[R_::L1 + perm<SIDE>(j)] * x[j];
+        }
+        y[0] = s0;
+        y[1] = s1;
+    }
+    // tangent rows t = 2..E-1: [-vt, 0, .., 1 (column t), .., 0] in the normal frame
+#pragma unroll
+    for (int t = 2; t < E; ++t) y[t] = zfix(-rec[R_::VT + t - 2] * x[0]) + x[perm<SIDE>(t)];
+    // row E: [LE0, LE1, L0[2..]] in the normal frame
+    {
+        real s = 0;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            int c = perm<SIDE>(j);
+            real m = c == 0 ? rec[R_::LE0] : (c == 1 ? rec[R_::LE1] : rec[R_::L0 + c]);
+            s = (j == 0) ? zfix(m * x[0]) : s + m * x[j];
+        }
+        y[E] = s;
+    }
+}
+
+// F = R f in the global frame: F_rot = R_rot f (j ascending), F_glob[g] = F_rot[perm(g)].
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void rightTransform(const real* rec, const real* f, real* F) {
+    typedef RoeRec<D> R_;
+    const int N = D + 2, E = N - 1;
+    if (!allFinite<real, N>(f)) { rightTransformDense<real, D, SIDE>(rec, f, F); return; }
+    real Fr[5];
+    // row 0: [1, 1, 0.., 1]
+    Fr[0] = zfix(f[0]) + f[1] + f[E];
+    // row 1: [lam0, vx, 0.., lamE]
+    Fr[1] = zfix(rec[R_::LAM0] * f[0]) + rec[R_::VX] * f[1] + rec[R_::LAME] * f[E];
+    // tangent rows t: [vt, vt, (1 at column t), vt]
+#pragma unroll
+    for (int t = 2; t < E; ++t) {
+        real vt = rec[R_::VT + t - 2];
+        Fr[t] = ((zfix(vt * f[0]) + vt * f[1]) + f[t]) + vt * f[E];
+    }
+    // row E: [H - c vx, .5 v^2, vt..., H + c vx]
+    {
+        real s = zfix(rec[R_::HM] * f[0]) + rec[R_::HV2] * f[1];
+#pragma unroll
+        for (int t = 2; t < E; ++t) s = s + rec[R_::VT + t - 2] * f[t];
+        Fr[E] = s + rec[R_::HP] * f[E];
+    }
+#pragma unroll
+    for (int g = 0; g < N; ++g) F[g] = Fr[perm<SIDE>(g)];
+}
+
+template <typename real, int D>
+__device__ __forceinline__ real roeEigenvalue(const real* rec, int i) {
+    typedef RoeRec<D> R_;
+    return i == 0 ? rec[R_::LAM0] : (i == D + 1 ? rec[R_::LAME] : rec[R_::VX]);
+}
+
+// Limited characteristic flux of one interface (res/Roe.cl:253-298).
+// sL, sR: stage states; dqL, dq, dqR: Delta-q-tilde at the faces before/at/after.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const real* sR, const real* dqL,
+                                        const real* dq, const real* dqR, real dt_dx, int lim, real* F) {
+    const int N = D + 2;
+    real avg[5], ft[5];
+#pragma unroll
+    for (int i = 0; i < N; ++i) avg[i] = (real).5 * (sR[i] + sL[i]);
+    leftTransform<real, D, SIDE>(rec, avg, ft);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        real eigenvalue = roeEigenvalue<real, D>(rec, i);
+        ft[i] = ft[i] * eigenvalue;
+        real rTilde, theta;
+        if (eigenvalue >= (real)0.) { rTilde = dqL[i] / dq[i]; theta = (real)1.; }
+        else { rTilde = dqR[i] / dq[i]; theta = (real)-1.; }
+        real phi = slopeLimiter<real>(lim, rTilde);
+        real epsilon = eigenvalue * dt_dx;
+        real deltaFluxTilde = eigenvalue * dq[i];
+        ft[i] = ft[i] - (real).5 * deltaFluxTilde * (theta + phi * (epsilon - theta));
+    }
+    rightTransform<real, D, SIDE>(rec, ft, F);
+}
+
+}  // namespace hgpu

@@ -144,7 +144,7 @@ def lognormal_grf(size=(256, 256, 256), xmin=(0., 0., 0.), xmax=(1., 1., 1.), ga
     kx = np.fft.rfftfreq(nx)[None, None, :]
     k2 = (2 * math.pi) ** 2 * (kx * kx + ky * ky + kz * kz)
     filt = np.exp(-.5 * k2 * corr_cells * corr_cells)
-    g = np.fft.irfftn(np.fft.rfftn(white) * filt, s=(nz, ny, nx))
+    g = np.fft.irfftn(np.fft.rfftn(white) * filt, s=(nz, ny, nx), axes=(0, 1, 2))
     g = (g - g.mean()) / g.std()
     rho = np.exp(sigma * g)
     rho = rho / rho.mean()

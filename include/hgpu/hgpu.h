@@ -149,6 +149,9 @@ int hgpu_config_default(hgpu_config* cfg);
 /* Human-readable name of a status code. */
 const char* hgpu_status_string(int status);
 
+/* Message of the last failure on the calling thread ("" if none). */
+const char* hgpu_last_error(void);
+
 /* Validate cfg and create a solver: replaces Solver::init (src/Solver/Solver.cpp:48-205),
  * i.e. NDRange setup, program build, initBuffers/initKernels and integrator selection.
  * Allocates every device buffer the step needs; later calls allocate nothing. */
@@ -200,6 +203,31 @@ int hgpu_set_graphs(hgpu_solver* s, int enabled);
 
 /* Number of kernels one step launches (for launch accounting). */
 int hgpu_kernels_per_step(const hgpu_solver* s, int* count);
+
+/* Make `device` current for this thread's later hgpu_create calls (the library
+ * carries its own CUDA runtime state).  Replica runs use one device per process. */
+int hgpu_select_device(int device);
+
+/* Advance nsteps like hgpu_update and return their device time in milliseconds,
+ * measured with CUDA events recorded on the solver's stream around the steps. */
+int hgpu_timed_update(hgpu_solver* s, int nsteps, float* ms);
+
+/* Per-kernel device time of nsteps updates run as plain launches, each launch
+ * bracketed by CUDA events on the solver's stream.  Fills up to cap entries. */
+typedef struct hgpu_kernel_time {
+    char name[32];
+    int launches;
+    double total_ms;
+} hgpu_kernel_time;
+int hgpu_profile_update(hgpu_solver* s, int nsteps, hgpu_kernel_time* out, int cap, int* count);
+
+/* Page-locked host buffers for state transfers (cudaHostAlloc / cudaFreeHost). */
+int hgpu_host_alloc(size_t bytes, void** ptr);
+int hgpu_host_free(void* ptr);
+
+/* Diagnostic: measured FP64 fused multiply-add issue rate of the current device
+ * (fma instructions per second, all SMs), the denominator of the FP64 roofline. */
+int hgpu_fp64_peak(double* fma_per_second);
 
 #ifdef __cplusplus
 }
