@@ -86,31 +86,35 @@ __host__ __device__ inline double bitsToDouble(unsigned long long b, bool isFloa
 enum : unsigned int { HEALTH_NONFINITE_DT = 1u, HEALTH_HLLC_NOBRANCH = 2u };
 
 // ---- slope limiters: res/SlopeLimiter.cl:5-68, min/max with fmin/fmax semantics ----
-// `real` is the program type; literals written `2.` in the reference are double, so the
-// FP64 instantiation is exact and the FP32 one follows the same expressions in float.
+// Literal types follow the reference source: `2.` is a double literal, so in the FP32
+// program those sub-expressions are evaluated in double and converted back, exactly
+// as C/OpenCL promote them; the FP64 program is unaffected.
 template <typename real>
 __device__ __forceinline__ real slopeLimiter(int lim, real r) {
+    typedef double W;
     switch (lim) {
-    case 0: return (real)0.;                                                         // DonorCell
-    case 1: return (real)1.;                                                         // LaxWendroff
-    case 2: return r;                                                                // BeamWarming
-    case 3: return (real).5 * ((real)1. + r);                                        // Fromm
-    case 4: return fmax((real)0., r) * ((real)3. * r + (real)1.) / ((r + (real)1.) * (r + (real)1.));  // CHARM
-    case 5: return fmax((real)0., (real)1.5 * (r + fabs(r)) / (r + (real)2.));      // HCUS
-    case 6: return fmax((real)0., (real)2. * (r + fabs(r)) / (r + (real)3.));       // HQUICK
-    case 7: return fmax((real)0., fmin((real)2. * r, fmin(((real)1. + (real)2. * r) / (real)3., (real)2.)));  // Koren
-    case 8: return fmax((real)0., fmin(r, (real)1.));                                // MinMod
-    case 9: return fmax((real)0., fmin(r, (real)1.5));                               // Oshker
-    case 10: return (real).5 * (r * r + r) / (r * r + r + (real)1.);                 // Ospre
-    case 11: return fmax((real)0., fmin((real)2. * r, fmin((real).25 + (real).75 * r, (real)4.)));  // Smart
-    case 12: return fmax((real)0., fmax(fmin((real)1.5 * r, (real)1.), fmin(r, (real)1.5)));       // Sweby
-    case 13: return fmax((real)0., fmin(fmin((real)2. * r, (real).75 + (real).25 * r), fmin((real).25 + (real).75 * r, (real)2.)));  // UMIST
-    case 14: return (r * r + r) / (r * r + (real)1.);                                // VanAlbada1
-    case 15: return (real)2. * r / (r * r + (real)1.);                               // VanAlbada2
-    case 16: return fmax((real)0., r) * (real)2. / ((real)1. + r);                  // VanLeer
-    case 17: return fmax((real)0., fmin((real)2., fmin((real).5 * ((real)1. + r), (real)2. * r)));  // MonotizedCentral
-    case 18: return fmax((real)0., fmax(fmin((real)1., (real)2. * r), fmin((real)2., r)));         // Superbee
-    case 19: return (real).5 * (r + (real)1.) * fmin((real)1., fmin((real)4. * r / (r + (real)1.), (real)4. / (r + (real)1.)));  // BarthJespersen
+    case 0: return (real)0.;                                                                     // DonorCell
+    case 1: return (real)1.;                                                                     // LaxWendroff
+    case 2: return r;                                                                            // BeamWarming
+    case 3: return (real)(.5 * (1. + (W)r));                                                     // Fromm
+    case 4: return (real)((W)(real)fmax((real)0., r) * (3. * (W)r + 1.) / (((W)r + 1.) * ((W)r + 1.)));  // CHARM
+    case 5: return (real)fmax((real)0., (real)(1.5 * (W)(r + (real)fabs(r)) / ((W)r + 2.)));     // HCUS
+    case 6: return (real)fmax((real)0., (real)(2. * (W)(r + (real)fabs(r)) / ((W)r + 3.)));      // HQUICK
+    case 7: return (real)fmax((real)0., (real)fmin(2. * (W)r, (W)(real)fmin((1. + 2. * (W)r) / 3., 2.)));  // Koren
+    case 8: return (real)fmax((real)0., (real)fmin(r, (real)1.));                                // MinMod
+    case 9: return (real)fmax((real)0., (real)fmin(r, (real)1.5));                               // Oshker
+    case 10: return (real)(.5 * (W)(r * r + r) / ((W)(r * r + r) + 1.));                         // Ospre
+    case 11: return (real)fmax((real)0., (real)fmin(2. * (W)r, (W)(real)fmin(.25 + .75 * (W)r, 4.)));  // Smart
+    case 12: return (real)fmax((real)0., (real)fmax((real)fmin(1.5 * (W)r, 1.), (real)fmin((W)r, 1.5)));  // Sweby
+    case 13: return (real)fmax((real)0., (real)fmin((real)fmin(2. * (W)r, .75 + .25 * (W)r),
+                                                    (real)fmin(.25 + .75 * (W)r, 2.)));         // UMIST
+    case 14: return (real)((W)(r * r + r) / ((W)(r * r) + 1.));                                 // VanAlbada1
+    case 15: return (real)(2. * (W)r / ((W)(r * r) + 1.));                                      // VanAlbada2
+    case 16: return (real)((W)(real)fmax((real)0., r) * 2. / (1. + (W)r));                      // VanLeer
+    case 17: return (real)fmax((real)0., (real)fmin(2., (W)(real)fmin(.5 * (1. + (W)r), 2. * (W)r)));  // MonotizedCentral
+    case 18: return (real)fmax((real)0., (real)fmax((real)fmin((real)1., (real)2. * r), (real)fmin((real)2., r)));  // Superbee
+    case 19: return (real)(.5 * ((W)r + 1.) *
+                           (W)(real)fmin((real)1., (real)fmin(4. * (W)r / ((W)r + 1.), 4. / ((W)r + 1.))));  // BarthJespersen
     }
     return (real)0.;
 }

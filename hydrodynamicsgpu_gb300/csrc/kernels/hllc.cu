@@ -30,12 +30,13 @@ struct Prim {
     real density, invDensity, v[3], velocitySq, energyTotal, pressure, enthalpyTotal;
 };
 
-// primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238), potential 0
+// primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238), potential 0.
+// `1. / densityL` and `(gamma - 1.) * ...` use double literals: FP32 promotes them.
 template <typename real, int D>
-__device__ __forceinline__ void primitives(const real* st, real gm1, Prim<real, D>& p) {
+__device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real, D>& p) {
     const int E = D + 1;
     p.density = st[0];
-    p.invDensity = (real)1. / p.density;
+    p.invDensity = (real)(1. / (double)p.density);
 #pragma unroll
     for (int k = 0; k < D; ++k) p.v[k] = st[1 + k] / p.density;
     p.velocitySq = p.v[0] * p.v[0];
@@ -44,34 +45,34 @@ __device__ __forceinline__ void primitives(const real* st, real gm1, Prim<real, 
     p.energyTotal = st[E] * p.invDensity;
     real energyKinetic = (real).5f * p.velocitySq;
     real energyInternal = p.energyTotal - energyKinetic;
-    p.pressure = gm1 * p.density * energyInternal;
+    p.pressure = (real)(((double)gamma - 1.) * (double)p.density * (double)energyInternal);
     p.enthalpyTotal = p.energyTotal + p.pressure * p.invDensity;
 }
 
 // sl, sr of one face (EulerHLLC.cl:85-97)
 template <typename real, int D, int SIDE>
-__device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, real gq, const real* __restrict__ state,
+__device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, double gq, const real* __restrict__ state,
                                          real* __restrict__ waves, long long c) {
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
-    const real gm1 = ph.gamma - (real)1.;
+    const double gm1 = (double)ph.gamma - 1.;
     Prim<real, D> L, R;
-    primitives<real, D>(sL, gm1, L);
-    primitives<real, D>(sR, gm1, R);
-    real cL = sqrt(gm1 * (L.enthalpyTotal - (real).5f * L.velocitySq));
-    real cR = sqrt(gm1 * (R.enthalpyTotal - (real).5f * R.velocitySq));
-    real pressureStar = fmax((real)0., (real).5f * (L.pressure + R.pressure) -
-                                           (real).5f * (R.v[0] - L.v[0]) * (real).5f * (L.density + R.density) *
-                                               (real).5f * (cL + cR));
-    real qL = pressureStar <= L.pressure ? (real)1. : sqrt((real)1. + gq * (pressureStar / L.pressure - (real)1.));
-    real qR = pressureStar <= R.pressure ? (real)1. : sqrt((real)1. + gq * (pressureStar / R.pressure - (real)1.));
+    primitives<real, D>(sL, ph.gamma, L);
+    primitives<real, D>(sR, ph.gamma, R);
+    real cL = (real)sqrt(gm1 * (double)(L.enthalpyTotal - .5f * L.velocitySq));
+    real cR = (real)sqrt(gm1 * (double)(R.enthalpyTotal - .5f * R.velocitySq));
+    real pressureStar = (real)fmax(0., (double)(.5f * (L.pressure + R.pressure) -
+                                                .5f * (R.v[0] - L.v[0]) * .5f * (L.density + R.density) * .5f *
+                                                    (cL + cR)));
+    real qL = pressureStar <= L.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / L.pressure) - 1.));
+    real qR = pressureStar <= R.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / R.pressure) - 1.));
     waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - cL * qL;
     waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + cR * qR;
 }
 
 template <typename real, int D>
-__global__ void __launch_bounds__(kThreads) hllcWaveKernel(Grid g, Phys<real> ph, real gq,
+__global__ void __launch_bounds__(kThreads) hllcWaveKernel(Grid g, Phys<real> ph, double gq,
                                                            const real* __restrict__ state, real* __restrict__ waves) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
@@ -120,10 +121,9 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
     loadRotated<real, D, SIDE>(stage, c, stR);
-    const real gm1 = ph.gamma - (real)1.;
     Prim<real, D> L, R;
-    primitives<real, D>(stL, gm1, L);
-    primitives<real, D>(stR, gm1, R);
+    primitives<real, D>(stL, ph.gamma, L);
+    primitives<real, D>(stR, ph.gamma, R);
     real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
     real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
     real fL[N], fR[N], flux[N];
@@ -205,8 +205,8 @@ __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph
 
 template <typename real>
 void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, cudaStream_t st) {
-    // (gamma + 1.) / (2. * gamma) is a per-program constant; computed once, identically
-    real gq = (ph.gamma + (real)1.) / ((real)2. * ph.gamma);
+    // (gamma + 1.) / (2. * gamma) is a per-program constant (double literals); computed once, identically
+    double gq = ((double)ph.gamma + 1.) / (2. * (double)ph.gamma);
     if (g.dim == 1) hllcWaveKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
     else if (g.dim == 2) hllcWaveKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
     else hllcWaveKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);

@@ -135,20 +135,24 @@ __device__ __forceinline__ real rightEntry(const real* rec, int i, int j) {
 // Dense forms, term for term as res/RoeEigenfieldLinear.cl:16-54 (used when an input
 // is not finite: then 0 * Inf/NaN terms matter).
 template <typename real, int D, int SIDE>
-__device__ __noinline__ void leftTransformDense(const real* rec, const real* x, real* y) {
+__device__ __forceinline__ void leftTransformDense(const real* rec, const real* x, real* y) {
     const int N = D + 2;
+#pragma unroll
     for (int i = 0; i < N; ++i) {
         real s = (real)0.f;
+#pragma unroll
         for (int j = 0; j < N; ++j) s = s + leftEntry<real, D>(rec, i, perm<SIDE>(j)) * x[j];
         y[i] = s;
     }
 }
 template <typename real, int D, int SIDE>
-__device__ __noinline__ void rightTransformDense(const real* rec, const real* f, real* F) {
+__device__ __forceinline__ void rightTransformDense(const real* rec, const real* f, real* F) {
     const int N = D + 2;
+#pragma unroll
     for (int g = 0; g < N; ++g) {
-        int i = perm<SIDE>(g);
+        const int i = perm<SIDE>(g);
         real s = (real)0.f;
+#pragma unroll
         for (int j = 0; j < N; ++j) s = s + rightEntry<real, D>(rec, i, j) * f[j];
         F[g] = s;
     }
@@ -230,7 +234,7 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
     const int N = D + 2;
     real avg[5], ft[5];
 #pragma unroll
-    for (int i = 0; i < N; ++i) avg[i] = (real).5 * (sR[i] + sL[i]);
+    for (int i = 0; i < N; ++i) avg[i] = (real)(.5 * (sR[i] + sL[i]));
     leftTransform<real, D, SIDE>(rec, avg, ft);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -242,7 +246,8 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
         real phi = slopeLimiter<real>(lim, rTilde);
         real epsilon = eigenvalue * dt_dx;
         real deltaFluxTilde = eigenvalue * dq[i];
-        ft[i] = ft[i] - (real).5 * deltaFluxTilde * (theta + phi * (epsilon - theta));
+        // `fluxTilde[i] -= .5 * deltaFluxTilde * (...)`: a double literal, so FP32 promotes here
+        ft[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta));
     }
     rightTransform<real, D, SIDE>(rec, ft, F);
 }
