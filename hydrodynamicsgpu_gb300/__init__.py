@@ -45,6 +45,7 @@ SIGNATURES = {
     "hgpu_fp64_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "hgpu_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "hgpu_host_free": (ctypes.c_int, [_P]),
+    "hgpu_cfl_timestep_noalloc": (ctypes.c_int, [_CFG, _P, ctypes.POINTER(ctypes.c_double), _P]),
 }
 
 

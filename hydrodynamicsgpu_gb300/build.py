@@ -24,6 +24,7 @@ SOURCES = {
     "kernels/hllc.cu": ["--fmad=false"],
     "kernels/combine.cu": ["--fmad=false"],
     "kernels/probe.cu": [],
+    "kernels/noalloc.cu": ["--fmad=false"],
     "host/solver.cu": [],
     "host/capi.cu": [],
 }

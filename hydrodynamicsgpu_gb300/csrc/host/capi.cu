@@ -9,6 +9,7 @@
 
 namespace hgpu {
 double measureFp64FmaRate();
+void setLastError(const std::string& msg);
 }
 
 struct hgpu_solver {
@@ -80,6 +81,8 @@ void runSteps(hgpu_solver* h, int nsteps) {
     }
 }
 }  // namespace
+
+void hgpu::setLastError(const std::string& msg) { g_lastError = msg; }
 
 extern "C" {
 

@@ -225,6 +225,21 @@ int hgpu_profile_update(hgpu_solver* s, int nsteps, hgpu_kernel_time* out, int c
 int hgpu_host_alloc(size_t bytes, void** ptr);
 int hgpu_host_free(void* ptr);
 
+/* CFL timestep of a ghost-filled device state without allocating device memory.
+ * No counterpart in the reference: it is for callers that cannot call cudaMalloc
+ * (hosts that own the whole device-memory budget through their own pool, code that
+ * runs where allocation is forbidden, plug-in hosts that only lend their buffers).
+ * Returns in *dt_out what Solver::calcTimestep would return for d_state (AoS, ghosts
+ * included, the precision of cfg), i.e. cfl * min over interior cells and axes of the
+ * cell timestep, and blocks until it is on the host.  Scratch is one fixed array
+ * inside the library (about 512 KiB on every GPU that loads it, kept until exit), so
+ * grids above 16,777,216 cells are rejected with HGPU_ERR_OOB.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU (different streams or threads at once) race and must be serialised by the
+ * caller.  `stream` is a cudaStream_t or NULL. */
+int hgpu_cfl_timestep_noalloc(const hgpu_config* cfg, const void* d_state, double* dt_out, void* stream);
+
 /* Diagnostic: measured FP64 fused multiply-add issue rate of the current device
  * (fma instructions per second, all SMs), the denominator of the FP64 roofline. */
 int hgpu_fp64_peak(double* fma_per_second);
