@@ -28,7 +28,7 @@ SOURCES = {
     "host/solver.cu": [],
     "host/capi.cu": [],
 }
-HEADERS = ["kernels/common.cuh", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h"]
+HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h"]
 
 
 def nvcc():

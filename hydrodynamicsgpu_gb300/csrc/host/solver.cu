@@ -269,7 +269,10 @@ void RungeKutta<real>::integrateZeroDeriv() {
 // ---------------- Solver ----------------
 template <typename real>
 Solver<real>::Solver(const ResolvedConfig& rc_) : rc(rc_) {
-    for (int i = 0; i < 3; ++i) ph.dx[i] = (real)rc.dx[i];
+    for (int i = 0; i < 3; ++i) {
+        ph.dx[i] = (real)rc.dx[i];
+        ph.rdx[i] = (real)1 / ph.dx[i];
+    }
     ph.gamma = (real)rc.gamma;
     ph.cfl = rc.cfg.cfl;
 }

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kThreads) derivCombineKernel(Grid g, Phys<real
 #pragma unroll
             for (int j = 0; j < N; ++j) {
                 const real* f = flux + ((long long)side * N + j) * g.V + c;
-                real t = (f[g.step[side]] - f[0]) / ph.dx[side];
+                real t = divByRecip(f[g.step[side]] - f[0], ph.dx[side], ph.rdx[side]);   // deltaFlux / dx[side]
                 d[j] = side == 0 ? zfix(-t) : d[j] - t;
             }
         }

@@ -12,6 +12,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fp64ops.cuh"
+
 namespace hgpu {
 
 // ---- grid geometry (reference layout: INDEX(x,y,z) = x + SX*(y + SY*z)) ----
@@ -85,37 +87,41 @@ __host__ __device__ inline double bitsToDouble(unsigned long long b, bool isFloa
 // ---- health word bits (hgpu_health) ----
 enum : unsigned int { HEALTH_NONFINITE_DT = 1u, HEALTH_HLLC_NOBRANCH = 2u };
 
-// ---- slope limiters: res/SlopeLimiter.cl:5-68, min/max with fmin/fmax semantics ----
+// ---- slope limiters: res/SlopeLimiter.cl:5-68, min/max with C-library fmin/fmax semantics ----
 // Literal types follow the reference source: `2.` is a double literal, so in the FP32
 // program those sub-expressions are evaluated in double and converted back, exactly
 // as C/OpenCL promote them; the FP64 program is unaffected.
 template <typename real>
 __device__ __forceinline__ real slopeLimiter(int lim, real r) {
     typedef double W;
+#define MN fminLibm
+#define MX fmaxLibm
     switch (lim) {
     case 0: return (real)0.;                                                                     // DonorCell
     case 1: return (real)1.;                                                                     // LaxWendroff
     case 2: return r;                                                                            // BeamWarming
     case 3: return (real)(.5 * (1. + (W)r));                                                     // Fromm
-    case 4: return (real)((W)(real)fmax((real)0., r) * (3. * (W)r + 1.) / (((W)r + 1.) * ((W)r + 1.)));  // CHARM
-    case 5: return (real)fmax((real)0., (real)(1.5 * (W)(r + (real)fabs(r)) / ((W)r + 2.)));     // HCUS
-    case 6: return (real)fmax((real)0., (real)(2. * (W)(r + (real)fabs(r)) / ((W)r + 3.)));      // HQUICK
-    case 7: return (real)fmax((real)0., (real)fmin(2. * (W)r, (W)(real)fmin((1. + 2. * (W)r) / 3., 2.)));  // Koren
-    case 8: return (real)fmax((real)0., (real)fmin(r, (real)1.));                                // MinMod
-    case 9: return (real)fmax((real)0., (real)fmin(r, (real)1.5));                               // Oshker
+    case 4: return (real)((W)(real)MX((real)0., r) * (3. * (W)r + 1.) / (((W)r + 1.) * ((W)r + 1.)));  // CHARM
+    case 5: return (real)MX((real)0., (real)(1.5 * (W)(r + (real)fabs(r)) / ((W)r + 2.)));       // HCUS
+    case 6: return (real)MX((real)0., (real)(2. * (W)(r + (real)fabs(r)) / ((W)r + 3.)));        // HQUICK
+    case 7: return (real)MX((real)0., (real)MN(2. * (W)r, (W)(real)MN((1. + 2. * (W)r) / 3., 2.)));  // Koren
+    case 8: return (real)MX((real)0., (real)MN(r, (real)1.));                                    // MinMod
+    case 9: return (real)MX((real)0., (real)MN(r, (real)1.5));                                   // Oshker
     case 10: return (real)(.5 * (W)(r * r + r) / ((W)(r * r + r) + 1.));                         // Ospre
-    case 11: return (real)fmax((real)0., (real)fmin(2. * (W)r, (W)(real)fmin(.25 + .75 * (W)r, 4.)));  // Smart
-    case 12: return (real)fmax((real)0., (real)fmax((real)fmin(1.5 * (W)r, 1.), (real)fmin((W)r, 1.5)));  // Sweby
-    case 13: return (real)fmax((real)0., (real)fmin((real)fmin(2. * (W)r, .75 + .25 * (W)r),
-                                                    (real)fmin(.25 + .75 * (W)r, 2.)));         // UMIST
+    case 11: return (real)MX((real)0., (real)MN(2. * (W)r, (W)(real)MN(.25 + .75 * (W)r, 4.)));  // Smart
+    case 12: return (real)MX((real)0., (real)MX((real)MN(1.5 * (W)r, 1.), (real)MN((W)r, 1.5)));  // Sweby
+    case 13: return (real)MX((real)0., (real)MN((real)MN(2. * (W)r, .75 + .25 * (W)r),
+                                                (real)MN(.25 + .75 * (W)r, 2.)));               // UMIST
     case 14: return (real)((W)(r * r + r) / ((W)(r * r) + 1.));                                 // VanAlbada1
     case 15: return (real)(2. * (W)r / ((W)(r * r) + 1.));                                      // VanAlbada2
-    case 16: return (real)((W)(real)fmax((real)0., r) * 2. / (1. + (W)r));                      // VanLeer
-    case 17: return (real)fmax((real)0., (real)fmin(2., (W)(real)fmin(.5 * (1. + (W)r), 2. * (W)r)));  // MonotizedCentral
-    case 18: return (real)fmax((real)0., (real)fmax((real)fmin((real)1., (real)2. * r), (real)fmin((real)2., r)));  // Superbee
+    case 16: return (real)((W)(real)MX((real)0., r) * 2. / (1. + (W)r));                        // VanLeer
+    case 17: return (real)MX((real)0., (real)MN(2., (W)(real)MN(.5 * (1. + (W)r), 2. * (W)r)));  // MonotizedCentral
+    case 18: return (real)MX((real)0., (real)MX((real)MN((real)1., (real)2. * r), (real)MN((real)2., r)));  // Superbee
     case 19: return (real)(.5 * ((W)r + 1.) *
-                           (W)(real)fmin((real)1., (real)fmin(4. * (W)r / ((W)r + 1.), 4. / ((W)r + 1.))));  // BarthJespersen
+                           (W)(real)MN((real)1., (real)MN(4. * (W)r / ((W)r + 1.), 4. / ((W)r + 1.))));  // BarthJespersen
     }
+#undef MN
+#undef MX
     return (real)0.;
 }
 

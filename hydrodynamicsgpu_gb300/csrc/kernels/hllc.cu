@@ -37,13 +37,14 @@ __device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real
     const int E = D + 1;
     p.density = st[0];
     p.invDensity = (real)(1. / (double)p.density);
+    // VELOCITY: m/rho, by the correction step on RN(1/rho) in FP64 (fp64ops.cuh)
 #pragma unroll
-    for (int k = 0; k < D; ++k) p.v[k] = st[1 + k] / p.density;
+    for (int k = 0; k < D; ++k) p.v[k] = divByRecip(st[1 + k], p.density, p.invDensity);
     p.velocitySq = p.v[0] * p.v[0];
 #pragma unroll
     for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + p.v[k] * p.v[k];
     p.energyTotal = st[E] * p.invDensity;
-    real energyKinetic = (real).5f * p.velocitySq;
+    real energyKinetic = halfOf(p.velocitySq);                          // .5f * velocitySq
     real energyInternal = p.energyTotal - energyKinetic;
     p.pressure = (real)(((double)gamma - 1.) * (double)p.density * (double)energyInternal);
     p.enthalpyTotal = p.energyTotal + p.pressure * p.invDensity;
@@ -60,11 +61,12 @@ __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, do
     Prim<real, D> L, R;
     primitives<real, D>(sL, ph.gamma, L);
     primitives<real, D>(sR, ph.gamma, R);
-    real cL = (real)sqrt(gm1 * (double)(L.enthalpyTotal - .5f * L.velocitySq));
-    real cR = (real)sqrt(gm1 * (double)(R.enthalpyTotal - .5f * R.velocitySq));
-    real pressureStar = (real)fmax(0., (double)(.5f * (L.pressure + R.pressure) -
-                                                .5f * (R.v[0] - L.v[0]) * .5f * (L.density + R.density) * .5f *
-                                                    (cL + cR)));
+    real cL = (real)sqrt(gm1 * (double)(L.enthalpyTotal - halfOf(L.velocitySq)));
+    real cR = (real)sqrt(gm1 * (double)(R.enthalpyTotal - halfOf(R.velocitySq)));
+    // .5f * (pL + pR) - .5f * (vR - vL) * .5f * (rhoL + rhoR) * .5f * (cL + cR), halvings exact
+    real pressureStar = (real)fmaxLibm(0., (double)(halfOf(L.pressure + R.pressure) -
+                                                    halfOf(halfOf(halfOf(R.v[0] - L.v[0])) * (L.density + R.density)) *
+                                                        (cL + cR)));
     real qL = pressureStar <= L.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / L.pressure) - 1.));
     real qR = pressureStar <= R.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / R.pressure) - 1.));
     waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - cL * qL;
@@ -100,11 +102,11 @@ __global__ void __launch_bounds__(kThreads) hllcDtKernel(Grid g, Phys<real> ph, 
             for (int side = 0; side < D; ++side) {
                 real srHere = waves[((long long)side * 2 + 1) * g.V + c];
                 real slNext = waves[((long long)side * 2 + 0) * g.V + c + g.step[side]];
-                real minLambda = (real)fmin(0., (double)slNext);
-                real maxLambda = (real)fmax(0., (double)srHere);
+                real minLambda = (real)fminLibm(0., (double)slNext);
+                real maxLambda = (real)fmaxLibm(0., (double)srHere);
                 real dum = ph.dx[side] / (maxLambda - minLambda);
                 if (dum != dum) nan = true;
-                result = fmin(result, dum);
+                result = fminLibm(result, dum);
             }
         }
         best = realBits(result);
@@ -144,21 +146,24 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fL[i];
     } else if (sl <= (real)0. && (real)0. <= sStar) {
-        real pressureLR = (real).5f * (L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
-                                       R.density * (sr - R.v[0]) * (sStar - R.v[0]));
-        flux[0] = sStar * (sl * stL[0] - fL[0]) / (sl - sStar);
-        flux[1] = (sStar * (sl * stL[1] - fL[1]) + sl * pressureLR) / (sl - sStar);
+        real pressureLR = halfOf(L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
+                                 R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        // every component divides by (sl - sStar): one reciprocal, then exact corrected quotients
+        real den = sl - sStar, rden = (real)1. / den;
+        flux[0] = divByRecip(sStar * (sl * stL[0] - fL[0]), den, rden);
+        flux[1] = divByRecip(sStar * (sl * stL[1] - fL[1]) + sl * pressureLR, den, rden);
 #pragma unroll
-        for (int k = 1; k < D; ++k) flux[1 + k] = sStar * (sl * stL[1 + k] - fL[1 + k]) / (sl - sStar);
-        flux[E] = (sStar * (sl * stL[E] - fL[E]) + sl * pressureLR * sStar) / (sl - sStar);
+        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(sStar * (sl * stL[1 + k] - fL[1 + k]), den, rden);
+        flux[E] = divByRecip(sStar * (sl * stL[E] - fL[E]) + sl * pressureLR * sStar, den, rden);
     } else if (sStar <= (real)0. && (real)0. <= sr) {
-        real pressureLR = (real).5f * (L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
-                                       R.density * (sr - R.v[0]) * (sStar - R.v[0]));
-        flux[0] = sStar * (sr * stR[0] - fR[0]) / (sr - sStar);
-        flux[1] = (sStar * (sr * stR[1] - fR[1]) + sr * pressureLR) / (sr - sStar);
+        real pressureLR = halfOf(L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
+                                 R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        real den = sr - sStar, rden = (real)1. / den;
+        flux[0] = divByRecip(sStar * (sr * stR[0] - fR[0]), den, rden);
+        flux[1] = divByRecip(sStar * (sr * stR[1] - fR[1]) + sr * pressureLR, den, rden);
 #pragma unroll
-        for (int k = 1; k < D; ++k) flux[1 + k] = sStar * (sr * stR[1 + k] - fR[1 + k]) / (sr - sStar);
-        flux[E] = (sStar * (sr * stR[E] - fR[E]) + sr * pressureLR * sStar) / (sr - sStar);
+        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(sStar * (sr * stR[1 + k] - fR[1 + k]), den, rden);
+        flux[E] = divByRecip(sStar * (sr * stR[E] - fR[E]) + sr * pressureLR * sStar, den, rden);
     } else if (sr <= (real)0.) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fR[i];

@@ -8,6 +8,7 @@ namespace hgpu {
 template <typename real>
 struct Phys {
     real dx[3];      // DX/DY/DZ as the program bakes them
+    real rdx[3];     // RN(1 / dx), for the exact division by dx (fp64ops.cuh divByRecip)
     real gamma;      // ((real)<defs value>)
     float cfl;
 };

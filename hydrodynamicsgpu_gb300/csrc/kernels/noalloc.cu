@@ -220,7 +220,10 @@ unsigned long long initBits(int solver, int dim) {
 template <typename real>
 void launchCfl(const ResolvedConfig& rc, int hllc, const void* state, long long blocks, cudaStream_t st) {
     Phys<real> ph;
-    for (int i = 0; i < 3; ++i) ph.dx[i] = (real)rc.dx[i];
+    for (int i = 0; i < 3; ++i) {
+        ph.dx[i] = (real)rc.dx[i];
+        ph.rdx[i] = (real)1 / ph.dx[i];
+    }
     ph.gamma = (real)rc.gamma;
     ph.cfl = rc.cfg.cfl;
     double gq = ((double)ph.gamma + 1.) / (2. * (double)ph.gamma);

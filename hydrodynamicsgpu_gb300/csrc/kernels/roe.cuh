@@ -12,6 +12,7 @@
 // global frame (see common.cuh for the zero/unit-coefficient rule).
 #pragma once
 #include "common.cuh"
+#include "fp64ops.cuh"
 
 namespace hgpu {
 
@@ -39,72 +40,92 @@ struct RoeRec {
 template <int SIDE>
 __device__ __forceinline__ constexpr int perm(int j) { return j == 1 ? 1 + SIDE : (j == 1 + SIDE ? 1 : j); }
 
-// Eigen basis of one interface (res/EulerRoe.cl:36-226 with solid == 0, potential == 0).
-// sL, sR: global-frame conserved states of the cells left/right of the face.
-template <typename real, int D, int SIDE>
-__device__ __forceinline__ void roeBasis(const real* sL, const real* sR, real gamma, real* rec) {
-    typedef RoeRec<D> R_;
-    const int N = D + 2, E = N - 1;
+// Per-cell part of the Roe eigenbasis (res/EulerRoe.cl:51-83 with solid == 0,
+// potential == 0): velocity, total enthalpy and Roe weight sqrt(rho).  Every face
+// uses these for its two cells; computing them once per cell is exact.
+template <typename real, int D>
+struct RoePrim {
+    real v[3];
+    real h;   // enthalpyTotal
+    real w;   // roeWeight = sqrt(density)
+};
+
+template <typename real, int D>
+__device__ __forceinline__ void roePrim(const real* s, real gamma, RoePrim<real, D>& P) {
+    const int E = D + 1;
     const real gm1 = gamma - (real)1.f;
-    real rhoL = sL[0], rhoR = sR[0];
-    // VELOCITY(ptr) = (m..., 0)/rho componentwise (res/include/HydroGPU/Euler.h:6-12)
-    real vL[3], vR[3];
+    real rho = s[0];
+    real invDensity = (real)1.f / rho;                                   // `1.f / density`
+    // VELOCITY(ptr) = (m..., 0)/rho componentwise (res/include/HydroGPU/Euler.h:6-12);
+    // m/rho by the correction step on RN(1/rho) (fp64ops.cuh) is the same quotient
 #pragma unroll
-    for (int k = 0; k < D; ++k) { vL[k] = sL[1 + k] / rhoL; vR[k] = sR[1 + k] / rhoR; }
+    for (int k = 0; k < D; ++k) P.v[k] = divByRecip(s[1 + k], rho, invDensity);
     // dot(v,v) over 4 components; the zero components add +0 to a non-negative sum
-    real vvL = vL[0] * vL[0], vvR = vR[0] * vR[0];
+    real vv = P.v[0] * P.v[0];
 #pragma unroll
-    for (int k = 1; k < D; ++k) { vvL = vvL + vL[k] * vL[k]; vvR = vvR + vR[k] * vR[k]; }
-    real invDensityL = (real)1.f / rhoL;
-    real energyTotalL = sL[E] * invDensityL;
-    real energyKineticL = (real).5f * vvL;
-    real energyInternalL = energyTotalL - energyKineticL;        // - potential (0)
-    real pressureL = gm1 * rhoL * energyInternalL;
-    real enthalpyTotalL = energyTotalL + pressureL * invDensityL;
-    real roeWeightL = sqrt(rhoL);
-    real invDensityR = (real)1.f / rhoR;
-    real energyTotalR = sR[E] * invDensityR;
-    real energyKineticR = (real).5f * vvR;
-    real energyInternalR = energyTotalR - energyKineticR;
-    real pressureR = gm1 * rhoR * energyInternalR;
-    real enthalpyTotalR = energyTotalR + pressureR * invDensityR;
-    real roeWeightR = sqrt(rhoR);
-    real norm = (real)1.f / (roeWeightL + roeWeightR);
+    for (int k = 1; k < D; ++k) vv = vv + P.v[k] * P.v[k];
+    real energyTotal = s[E] * invDensity;
+    real energyKinetic = halfOf(vv);                                     // .5f * dot(v, v)
+    real energyInternal = energyTotal - energyKinetic;                   // - potential (0)
+    real pressure = gm1 * rho * energyInternal;
+    P.h = energyTotal + pressure * invDensity;
+    P.w = sqrt(rho);
+}
+
+// Per-face part (res/EulerRoe.cl:85-226): Roe averages, eigenvalues, R and L.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void roeBasisFromPrim(const RoePrim<real, D>& L, const RoePrim<real, D>& R, real gamma,
+                                                 real* rec) {
+    typedef RoeRec<D> R_;
+    const int E = D + 1;
+    const real gm1 = gamma - (real)1.f;
+    real norm = (real)1.f / (L.w + R.w);
     real v[3];
 #pragma unroll
-    for (int k = 0; k < D; ++k) v[k] = (roeWeightL * vL[k] + roeWeightR * vR[k]) * norm;
-    real enthalpyTotal = (roeWeightL * enthalpyTotalL + roeWeightR * enthalpyTotalR) * norm;
+    for (int k = 0; k < D; ++k) v[k] = (L.w * L.v[k] + R.w * R.v[k]) * norm;
+    real enthalpyTotal = (L.w * L.h + R.w * R.h) * norm;
     real velocitySq = v[0] * v[0];
 #pragma unroll
     for (int k = 1; k < D; ++k) velocitySq = velocitySq + v[k] * v[k];
-    real c = sqrt((enthalpyTotal - (real).5f * velocitySq) * gm1);  // - energyPotential (0)
+    real c = sqrt((enthalpyTotal - halfOf(velocitySq)) * gm1);          // - energyPotential (0)
     // rotate: normal velocity first (res/EulerRoe.cl:101-110)
     real vx = v[SIDE];
     real vt[2] = {0, 0};
     if (D > 1) vt[0] = (SIDE == 1) ? v[0] : v[1];
     if (D > 2) vt[1] = (SIDE == 2) ? v[0] : v[2];
+    real cvx = c * vx;
     rec[R_::LAM0] = vx - c;
     rec[R_::VX] = vx;
     rec[R_::LAME] = vx + c;
-    rec[R_::HM] = enthalpyTotal - c * vx;
-    rec[R_::HV2] = (real).5f * velocitySq;
-    rec[R_::HP] = enthalpyTotal + c * vx;
+    rec[R_::HM] = enthalpyTotal - cvx;
+    rec[R_::HV2] = halfOf(velocitySq);
 #pragma unroll
     for (int t = 0; t < D - 1; ++t) rec[R_::VT + t] = vt[t];
+    rec[R_::HP] = enthalpyTotal + cvx;
     real invDenom = (real).5f / (c * c);
-    real h = (real).5f * gm1;
-    rec[R_::L0 + 0] = (h * velocitySq + c * vx) * invDenom;
-    rec[R_::L0 + 1] = -(c + gm1 * vx) * invDenom;
+    real hv = (real).5f * gm1 * velocitySq;                              // .5f * (gamma - 1.f) * velocitySq
+    real gvx = gm1 * vx;
+    rec[R_::L0 + 0] = (hv + cvx) * invDenom;
+    rec[R_::L0 + 1] = -(c + gvx) * invDenom;
 #pragma unroll
     for (int t = 0; t < D - 1; ++t) rec[R_::L0 + 2 + t] = -gm1 * vt[t] * invDenom;
     rec[R_::L0 + E] = gm1 * invDenom;
     rec[R_::L1 + 0] = (real)1.f - gm1 * velocitySq * invDenom;
-    rec[R_::L1 + 1] = gm1 * vx * (real)2.f * invDenom;
+    rec[R_::L1 + 1] = gvx * (real)2.f * invDenom;
 #pragma unroll
     for (int t = 0; t < D - 1; ++t) rec[R_::L1 + 2 + t] = gm1 * vt[t] * (real)2.f * invDenom;
     rec[R_::L1 + E] = -gm1 * (real)2.f * invDenom;
-    rec[R_::LE0] = (h * velocitySq - c * vx) * invDenom;
-    rec[R_::LE1] = (c - gm1 * vx) * invDenom;
+    rec[R_::LE0] = (hv - cvx) * invDenom;
+    rec[R_::LE1] = (c - gvx) * invDenom;
+}
+
+// Eigen basis of one interface from the two cell states.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void roeBasis(const real* sL, const real* sR, real gamma, real* rec) {
+    RoePrim<real, D> L, R;
+    roePrim<real, D>(sL, gamma, L);
+    roePrim<real, D>(sR, gamma, R);
+    roeBasisFromPrim<real, D, SIDE>(L, R, gamma, rec);
 }
 
 // Normal-frame matrix entries, including the structural zeros and ones.
@@ -231,23 +252,32 @@ __device__ __forceinline__ real roeEigenvalue(const real* rec, int i) {
 template <typename real, int D, int SIDE>
 __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const real* sR, const real* dqL,
                                         const real* dq, const real* dqR, real dt_dx, int lim, real* F) {
+    typedef RoeRec<D> R_;
     const int N = D + 2;
     real avg[5], ft[5];
 #pragma unroll
-    for (int i = 0; i < N; ++i) avg[i] = (real)(.5 * (sR[i] + sL[i]));
+    for (int i = 0; i < N; ++i) avg[i] = (real)halfOf((double)(sR[i] + sL[i]));    // .5 * (stateR + stateL)
     leftTransform<real, D, SIDE>(rec, avg, ft);
+    // waves 1..N-2 share the eigenvalue vx: their epsilon and theta are the same values
+    const real vx = rec[R_::VX];
+    const bool midUp = geZero(vx);
+    const real midTheta = midUp ? (real)1. : (real)-1.;
+    const real midEps = vx * dt_dx;
+    const real midEpsTheta = midEps - midTheta;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
+        const bool mid = i > 0 && i < N - 1;
         real eigenvalue = roeEigenvalue<real, D>(rec, i);
         ft[i] = ft[i] * eigenvalue;
-        real rTilde, theta;
-        if (eigenvalue >= (real)0.) { rTilde = dqL[i] / dq[i]; theta = (real)1.; }
-        else { rTilde = dqR[i] / dq[i]; theta = (real)-1.; }
+        bool up = mid ? midUp : geZero(eigenvalue);
+        real rTilde = (up ? dqL[i] : dqR[i]) / dq[i];
+        real theta = mid ? midTheta : (up ? (real)1. : (real)-1.);
         real phi = slopeLimiter<real>(lim, rTilde);
-        real epsilon = eigenvalue * dt_dx;
+        real epsMinusTheta = mid ? midEpsTheta : eigenvalue * dt_dx - theta;
         real deltaFluxTilde = eigenvalue * dq[i];
-        // `fluxTilde[i] -= .5 * deltaFluxTilde * (...)`: a double literal, so FP32 promotes here
-        ft[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta));
+        // `fluxTilde[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta))`
+        if (sizeof(real) == 8) ft[i] = ft[i] - halfOf(deltaFluxTilde) * (theta + phi * epsMinusTheta);
+        else ft[i] -= .5 * deltaFluxTilde * (theta + phi * epsMinusTheta);   // double literal: FP32 promotes
     }
     rightTransform<real, D, SIDE>(rec, ft, F);
 }
