@@ -46,6 +46,19 @@ SIGNATURES = {
     "hgpu_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "hgpu_host_free": (ctypes.c_int, [_P]),
     "hgpu_cfl_timestep_noalloc": (ctypes.c_int, [_CFG, _P, ctypes.POINTER(ctypes.c_double), _P]),
+    "hgpu_batch_create": (ctypes.c_int, [_CFG, ctypes.c_int, ctypes.POINTER(_P)]),
+    "hgpu_batch_destroy": (ctypes.c_int, [_P]),
+    "hgpu_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
+                                       ctypes.POINTER(ctypes.c_int)]),
+    "hgpu_batch_set_state": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t]),
+    "hgpu_batch_get_state": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t]),
+    "hgpu_batch_update": (ctypes.c_int, [_P, ctypes.c_int]),
+    "hgpu_batch_timed_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "hgpu_batch_dts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "hgpu_batch_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "hgpu_batch_get_tuning": (ctypes.c_int, [_P, _P]),
+    "hgpu_batch_set_tuning": (ctypes.c_int, [_P, _P]),
+    "hgpu_batch_autotune": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
 }
 
 
@@ -243,3 +256,81 @@ class Solver:
             json.dump({"size": list(self.cfg.size), "dtype": np.dtype(self.dtype).name, "channels": names,
                        "frame": self.frame}, f)
         return names
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int), ("tile_z", ctypes.c_int),
+                ("staged", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+
+
+class Batch:
+    """Many independent problems (same solver/dim/integrator/limiter/precision, their
+    own sizes, domains, cfl and boundaries) advanced together in persistent launches."""
+
+    def __init__(self, cfgs):
+        arr = (HgpuConfig * len(cfgs))(*cfgs)
+        self.cfgs = list(cfgs)
+        h = ctypes.c_void_p()
+        check(lib().hgpu_batch_create(arr, len(cfgs), ctypes.byref(h)))
+        self.h = h
+        self.dtype = np.float32 if cfgs[0].precision == FP32 else np.float64
+        self.n = len(cfgs)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def count(self, p):
+        return _abi.config_count(self.cfgs[p])
+
+    def set_state(self, p, state):
+        a = np.ascontiguousarray(state, dtype=self.dtype).reshape(-1)
+        check(lib().hgpu_batch_set_state(self.h, int(p), a.ctypes.data, a.size))
+
+    def get_state(self, p):
+        a = np.empty(self.count(p), dtype=self.dtype)
+        check(lib().hgpu_batch_get_state(self.h, int(p), a.ctypes.data, a.size))
+        return a
+
+    def update(self, nsteps=1):
+        check(lib().hgpu_batch_update(self.h, int(nsteps)))
+
+    def timed_update(self, nsteps):
+        ms = ctypes.c_float()
+        check(lib().hgpu_batch_timed_update(self.h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def dts(self):
+        out = (ctypes.c_double * self.n)()
+        check(lib().hgpu_batch_dts(self.h, out, self.n))
+        return np.array(out[:])
+
+    def health(self):
+        f = ctypes.c_uint32()
+        check(lib().hgpu_batch_health(self.h, ctypes.byref(f)))
+        return f.value
+
+    def info(self):
+        n, cells, k = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int()
+        check(lib().hgpu_batch_info(self.h, ctypes.byref(n), ctypes.byref(cells), ctypes.byref(k)))
+        return n.value, cells.value, k.value
+
+    def tuning(self):
+        t = BatchTuning()
+        check(lib().hgpu_batch_get_tuning(self.h, ctypes.byref(t)))
+        return (t.tile_x, t.tile_y, t.tile_z, t.staged, t.blocks_per_sm)
+
+    def set_tuning(self, tile=(32, 8, 1), staged=1, blocks_per_sm=0):
+        t = BatchTuning(tile[0], tile[1], tile[2], staged, blocks_per_sm)
+        check(lib().hgpu_batch_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, cache_path=None, steps=2):
+        check(lib().hgpu_batch_autotune(self.h, cache_path.encode() if cache_path else None, int(steps)))
+        return self.tuning()

@@ -25,10 +25,13 @@ SOURCES = {
     "kernels/combine.cu": ["--fmad=false"],
     "kernels/probe.cu": [],
     "kernels/noalloc.cu": ["--fmad=false"],
+    "kernels/batch.cu": ["--fmad=false"],
+    "host/batch_solver.cu": [],
     "host/solver.cu": [],
     "host/capi.cu": [],
 }
-HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h"]
+HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
+           "kernels/combine_cells.cuh", "kernels/batch.h", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h"]
 
 
 def nvcc():

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "batch_solver.h"
 #include "solver.h"
 
 namespace hgpu {
@@ -299,6 +300,91 @@ int hgpu_host_alloc(size_t bytes, void** ptr) {
 int hgpu_host_free(void* ptr) {
     return guarded([&]() {
         if (ptr) hgpu::cudaCheck(cudaFreeHost(ptr), "cudaFreeHost");
+        return (int)HGPU_OK;
+    });
+}
+
+struct hgpu_batch {
+    std::unique_ptr<hgpu::BatchBase> b;
+};
+
+int hgpu_batch_create(const hgpu_config* cfgs, int nproblems, hgpu_batch** out) {
+    if (!cfgs || !out || nproblems <= 0) return fail(HGPU_ERR_ARG, "bad argument");
+    *out = nullptr;
+    return guarded([&]() {
+        std::unique_ptr<hgpu_batch> h(new hgpu_batch());
+        h->b = hgpu::createBatch(std::vector<hgpu_config>(cfgs, cfgs + nproblems));
+        *out = h.release();
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_batch_destroy(hgpu_batch* b) {
+    if (!b) return HGPU_OK;
+    return guarded([&]() {
+        if (b->b && b->b->stream) cudaStreamSynchronize(b->b->stream);
+        delete b;
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_batch_info(const hgpu_batch* b, int* nproblems, long long* total_cells, int* kernels_per_step) {
+    if (!b) return fail(HGPU_ERR_ARG, "null handle");
+    if (nproblems) *nproblems = b->b->problems();
+    if (total_cells) *total_cells = b->b->totalCells();
+    if (kernels_per_step) *kernels_per_step = b->b->kernelsPerStep();
+    return HGPU_OK;
+}
+
+int hgpu_batch_set_state(hgpu_batch* b, int problem, const void* host_state, size_t count) {
+    if (!b || !host_state) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { b->b->setState(problem, host_state, count); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_get_state(hgpu_batch* b, int problem, void* host_state, size_t count) {
+    if (!b || !host_state) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { b->b->getState(problem, host_state, count); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_update(hgpu_batch* b, int nsteps) {
+    if (!b || nsteps < 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() { b->b->run(nsteps); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_timed_update(hgpu_batch* b, int nsteps, float* ms) {
+    if (!b || !ms || nsteps < 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() { *ms = b->b->timedRun(nsteps); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_dts(hgpu_batch* b, double* dts, int n) {
+    if (!b || !dts) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { b->b->dts(dts, n); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_health(hgpu_batch* b, uint32_t* flags) {
+    if (!b || !flags) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { *flags = b->b->readHealth(); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_get_tuning(const hgpu_batch* b, hgpu_batch_tuning* t) {
+    if (!b || !t) return fail(HGPU_ERR_ARG, "null argument");
+    hgpu::BatchTuning tu = b->b->tuning();
+    *t = {tu.tx, tu.ty, tu.tz, tu.staged, tu.blocksPerSM};
+    return HGPU_OK;
+}
+
+int hgpu_batch_set_tuning(hgpu_batch* b, const hgpu_batch_tuning* t) {
+    if (!b || !t) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        b->b->setTuning({t->tile_x, t->tile_y, t->tile_z, t->staged, t->blocks_per_sm});
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_batch_autotune(hgpu_batch* b, const char* cache_path, int steps) {
+    if (!b || steps <= 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        b->b->autotune(cache_path ? std::string(cache_path) : std::string(), steps);
         return (int)HGPU_OK;
     });
 }

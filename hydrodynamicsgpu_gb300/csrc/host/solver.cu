@@ -165,11 +165,7 @@ void ForwardEuler<real>::integrateZeroDeriv() {
 template <typename real>
 RungeKutta<real>::RungeKutta(Solver<real>* s, int tableau) : Integrator<real>(s), tableau_(tableau) {
     order_ = tableauOrder(tableau);
-    for (int m = 0; m < order_; ++m)
-        for (int k = 0; k <= m; ++k) {
-            double a = tableauAlpha(tableau, m, k);
-            if (a != 0.0 && a != 1.0) alphaIsBinary_ = false;
-        }
+    alphaIsBinary_ = tableauAlphaIsBinary(tableau);
     buildPlans();
 }
 
@@ -178,10 +174,12 @@ RungeKutta<real>::RungeKutta(Solver<real>* s, int tableau) : Integrator<real>(s)
 // its alpha(m,k) u^(k) and beta(m,k) dt d^(k) terms are added, in that order, to its
 // partial sum.  A row whose sum is still exactly u^n (alpha = 1, nothing else) is
 // not materialised: it aliases the state buffer, which holds u^n until the last
-// stage writes the new state into it.
+// stage writes the new state into it.  Slot 0 is the state; slots 1..nslots are work
+// buffers of the state's size.  Pointers are filled in by the caller.
 template <typename real>
-void RungeKutta<real>::buildPlans() {
-    const int order = order_;
+StagePlans<real> buildStagePlans(int tableau) {
+    StagePlans<real> out;
+    const int order = tableauOrder(tableau);
     struct Row { int slot = -1; bool alias0 = false; };
     std::vector<Row> rows(order);
     std::vector<bool> slotBusy(8, false);
@@ -193,14 +191,12 @@ void RungeKutta<real>::buildPlans() {
         throw std::logic_error("out of Runge-Kutta work slots");
     };
     int inSlot = 0;
-    plans_.clear();
-    inputSlot_.clear();
     for (int k = 0; k < order; ++k) {
         CombinePlan<real> plan{};
         plan.fe = 0;
         plan.in = inSlot;
         for (int m = k; m < order; ++m) {
-            double a = tableauAlpha(tableau_, m, k), b = tableauBeta(tableau_, m, k);
+            double a = tableauAlpha(tableau, m, k), b = tableauBeta(tableau, m, k);
             if (a == 0.0 && b == 0.0) continue;
             Row& r = rows[m];
             bool fresh = r.slot < 0 && !r.alias0;
@@ -225,14 +221,33 @@ void RungeKutta<real>::buildPlans() {
             if (plan.nops >= 4) throw std::logic_error("too many rows in a stage");
             plan.ops[plan.nops++] = op;
         }
-        plans_.push_back(plan);
-        inputSlot_.push_back(inSlot);
+        out.plans.push_back(plan);
+        out.inputSlot.push_back(inSlot);
         if (k < order - 1) {
             if (inSlot != 0) slotBusy[inSlot] = false;   // u^(k) is consumed by stage k
             inSlot = rows[k].alias0 ? 0 : rows[k].slot;
         }
     }
-    nslots_ = maxSlot;
+    out.nslots = maxSlot;
+    return out;
+}
+
+bool tableauAlphaIsBinary(int tableau) {
+    int order = tableauOrder(tableau);
+    for (int m = 0; m < order; ++m)
+        for (int k = 0; k <= m; ++k) {
+            double a = tableauAlpha(tableau, m, k);
+            if (a != 0.0 && a != 1.0) return false;
+        }
+    return true;
+}
+
+template <typename real>
+void RungeKutta<real>::buildPlans() {
+    StagePlans<real> sp = buildStagePlans<real>(tableau_);
+    plans_ = sp.plans;
+    inputSlot_ = sp.inputSlot;
+    nslots_ = sp.nslots;
     work_.clear();
     size_t bytes = sizeof(real) * (size_t)this->solver->rc.grid.V * this->solver->rc.numStates;
     for (int i = 0; i < nslots_; ++i) work_.emplace_back(bytes, true);
@@ -489,6 +504,8 @@ std::unique_ptr<SolverBase> createSolver(const hgpu_config& cfg) {
     return makeSolver<double>(rc);
 }
 
+template StagePlans<double> buildStagePlans<double>(int);
+template StagePlans<float> buildStagePlans<float>(int);
 template class Solver<double>;
 template class Solver<float>;
 template class ForwardEuler<double>;

@@ -84,6 +84,16 @@ private:
 
 template <typename real> class Solver;
 
+// Runge-Kutta stage plans of a tableau (see buildStagePlans in solver.cu)
+template <typename real>
+struct StagePlans {
+    std::vector<CombinePlan<real>> plans;   // one per stage, slot pointers unset
+    std::vector<int> inputSlot;             // stage k reads u^(k) from this slot
+    int nslots = 0;                         // work buffers needed besides the state
+};
+template <typename real> StagePlans<real> buildStagePlans(int tableau);
+bool tableauAlphaIsBinary(int tableau);
+
 // ---------------- Integrator (include/HydroGPU/Integrator/Integrator.h:13-17) ----------------
 template <typename real>
 class Integrator {

@@ -11,52 +11,15 @@
 //    term before beta term, starting from +0, so every sum is bit-identical;
 //  * findMinTimestep's host read and `dt * cfl` (Solver.cpp:466-516): dt is
 //    finalised on the device, with dt/dx and beta*dt, for the whole step.
+#include "combine_cells.cuh"
 #include "kernels.h"
 
 namespace hgpu {
-
-// ---------------- tableaus: include/HydroGPU/Integrator/RungeKutta.h:129-294 ----------------
-#define HGPU_TABLE_A                                                                                         \
-    {{{1}},                                                                                                  \
-     {{1, 0}, {1, 0}},                                                                                       \
-     {{1, 0}, {1, 0}},                                                                                       \
-     {{1, 0}, {1, 0}},                                                                                       \
-     {{1, 0, 0}, {1, 0, 0}, {1, 0, 0}},                                                                      \
-     {{1, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 0, 0}},                                               \
-     {{1, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 0, 0}},                                               \
-     {{1, 0}, {.5, .5}},                                                                                     \
-     {{1, 0}, {1, 0}},                                                                                       \
-     {{1, 0, 0}, {3. / 4., 1. / 4., 0}, {1. / 3., 2. / 3., 0}},                                              \
-     {{1, 0, 0, 0}, {649. / 1600., 951. / 1600., 0, 0},                                                      \
-      {53989. / 2500000., 4806213. / 20000000., 23619. / 32000., 0},                                         \
-      {1. / 5., 6127. / 30000., 7873. / 30000., 1. / 3.}},                                                   \
-     {{1, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 0, 0}, {-1. / 3., 1. / 3., 2. / 3., 1. / 3.}}}
-#define HGPU_TABLE_B                                                                                         \
-    {{{1}},                                                                                                  \
-     {{.5, 0}, {0, 1}},                                                                                      \
-     {{1, 0}, {.5, .5}},                                                                                     \
-     {{2. / 3., 0}, {1. / 4., 3. / 4.}},                                                                     \
-     {{.5, 0, 0}, {-1, 2, 0}, {1. / 6., 2. / 6., 1. / 6.}},                                                  \
-     {{.5, 0, 0, 0}, {0, .5, 0, 0}, {0, 0, 1, 0}, {1. / 6., 2. / 6., 2. / 6., 1. / 6.}},                     \
-     {{1. / 3., 0, 0, 0}, {-1. / 3., 0, 0, 0}, {1, -1, 1, 0}, {1. / 8., 3. / 8., 3. / 8., 1. / 8.}},         \
-     {{1, 0}, {0, .5}},                                                                                      \
-     {{-20, 0}, {41. / 40., -1. / 40.}},                                                                     \
-     {{1, 0, 0}, {0, 1. / 4., 0}, {0, 0, 2. / 3.}},                                                          \
-     {{.5, 0, 0, 0}, {-10890423. / 25193600., 5000. / 7873, 0, 0},                                           \
-      {-102261. / 5000000., -5121. / 20000., 7873. / 10000., 0}, {1. / 10., 1. / 6., 0, 1. / 6.}},          \
-     {{.5, 0, 0, 0}, {0, .5, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1. / 6.}}}
-#define HGPU_TABLE_ORDER {1, 2, 2, 2, 3, 4, 4, 2, 2, 3, 4, 4}
 
 namespace {
 const double kA[12][4][4] = HGPU_TABLE_A;
 const double kB[12][4][4] = HGPU_TABLE_B;
 const int kOrder[12] = HGPU_TABLE_ORDER;
-__constant__ double cA[12][4][4] = HGPU_TABLE_A;
-__constant__ double cB[12][4][4] = HGPU_TABLE_B;
-__constant__ int cOrder[12] = HGPU_TABLE_ORDER;
-__device__ __forceinline__ int kOrderDev(int i) { return cOrder[i]; }
-__device__ __forceinline__ double kAlphaDev(int i, int m, int k) { return cA[i][m][k]; }
-__device__ __forceinline__ double kBetaDev(int i, int m, int k) { return cB[i][m][k]; }
 }  // namespace
 
 int tableauOrder(int integ) { return kOrder[integ]; }
@@ -69,47 +32,10 @@ constexpr int kThreads = 256;
 inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
 // ---------------- ghost fill ----------------
-// thread = one line along `axis`; handles all N states, min side then max side.
-// In 1D the reference's Mirror/Reflect/FreeFlow kernels have no range guard and
-// only work-item 0 addresses the buffer; that work-item is what runs here.
 template <typename real>
 __global__ void __launch_bounds__(kThreads) boundaryKernel(Grid g, int axis, int N, int mMin, int mMax,
                                                            real* __restrict__ state) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int A = axis == 0 ? 1 : 0, B = axis == 2 ? 1 : 2;   // transverse axes
-    long long nA = g.S[A], nB = g.S[B];
-    if (g.dim == 1) { nA = 1; nB = 1; }
-    if (t >= nA * nB) return;
-    int a = (int)(t % nA), b = (int)(t / nA);
-    int c[3];
-    c[A] = a; c[B] = b; c[axis] = 0;
-    long long base = c[0] + (long long)g.S[0] * (c[1] + (long long)g.S[1] * c[2]);
-    long long st = g.step[axis];
-    int S = g.S[axis];
-    for (int j = 0; j < N; ++j) {
-        real* p = state + j;
-#define AT(k) p[(long long)N * (base + (long long)(k) * st)]
-        for (int side = 0; side < 2; ++side) {
-            int m = side == 0 ? mMin : mMax;
-            if (m < 0) continue;
-            // Euler::stateGetBoundaryKernelForBoundaryMethod: MIRROR reflects the normal momentum
-            int kern = m == 0 ? 0 : (m == 1 ? ((axis + 1 == j) ? 2 : 1) : 3);
-            if (kern == 0) {                                  // periodic
-                if (side == 0) { AT(0) = AT(S - 4); AT(1) = AT(S - 3); }
-                else { AT(S - 2) = AT(2); AT(S - 1) = AT(3); }
-            } else if (kern == 1) {                           // mirror
-                if (side == 0) { AT(0) = AT(3); AT(1) = AT(2); }
-                else { AT(S - 1) = AT(S - 4); AT(S - 2) = AT(S - 3); }
-            } else if (kern == 2) {                           // reflect
-                if (side == 0) { AT(0) = -AT(3); AT(1) = -AT(2); }
-                else { AT(S - 1) = -AT(S - 4); AT(S - 2) = -AT(S - 3); }
-            } else {                                          // free flow
-                if (side == 0) { real v = AT(2); AT(1) = v; AT(0) = v; }
-                else { real v = AT(S - 3); AT(S - 2) = v; AT(S - 1) = v; }
-            }
-        }
-#undef AT
-    }
+    boundaryLine<real>(g, axis, N, mMin, mMax, state, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------- flux divergence + stage combine ----------------
@@ -117,109 +43,26 @@ template <typename real, int D>
 __global__ void __launch_bounds__(kThreads) derivCombineKernel(Grid g, Phys<real> ph, const real* __restrict__ flux,
                                                                CombinePlan<real> plan,
                                                                const StepConst<real>* __restrict__ sc) {
-    const int N = D + 2;
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    real d[N];
-    // calcFluxDeriv: interior cells only, deriv[j] -= (F[i+1] - F[i]) / dx, sides ascending, from 0
-    if (inRange(g, x, y, z, 2, 2)) {
-#pragma unroll
-        for (int side = 0; side < D; ++side) {
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                const real* f = flux + ((long long)side * N + j) * g.V + c;
-                real t = divByRecip(f[g.step[side]] - f[0], ph.dx[side], ph.rdx[side]);   // deltaFlux / dx[side]
-                d[j] = side == 0 ? zfix(-t) : d[j] - t;
-            }
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < N; ++j) d[j] = (real)0.;
-    }
-    if (plan.fe) {                                            // ForwardEuler::integrate: state += deriv * dt
-        real dt = sc->dt;
-        real* s = plan.slot[0] + (long long)N * c;
-#pragma unroll
-        for (int j = 0; j < N; ++j) s[j] = s[j] + d[j] * dt;
-        return;
-    }
-    real u[N];
-    const real* in = plan.slot[plan.in] + (long long)N * c;
-#pragma unroll
-    for (int j = 0; j < N; ++j) u[j] = in[j];
-    for (int o = 0; o < plan.nops; ++o) {
-        const CombineOp<real>& op = plan.ops[o];
-        real v[N];
-        bool empty = op.prior < 0;
-        if (!empty) {
-            const real* p = plan.slot[op.prior] + (long long)N * c;
-#pragma unroll
-            for (int j = 0; j < N; ++j) v[j] = op.priorAlias ? zfix(p[j]) : p[j];
-        }
-        if (op.hasAlpha) {
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                real t = op.alphaIsOne ? u[j] : u[j] * op.alpha;
-                v[j] = empty ? zfix(t) : v[j] + t;
-            }
-            empty = false;
-        }
-        if (op.hasBeta) {
-            real cf = sc->coef[op.brow][op.bcol];
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                real t = d[j] * cf;
-                v[j] = empty ? zfix(t) : v[j] + t;
-            }
-        }
-        real* o_ = plan.slot[op.out] + (long long)N * c;
-#pragma unroll
-        for (int j = 0; j < N; ++j) o_[j] = v[j];
-    }
+    derivCombineCell<real, D>(g, ph, flux, plan, *sc, c, x, y, z, 0);
 }
 
-// Self-gravity pass with a zero potential and a Runge-Kutta integrator: every deriv
-// is +0, so each stage state is the alpha-combination of earlier ones
-// (SelfGravitation.cpp:100-124 through RungeKutta.h:59-125).  Element-wise.
 template <typename real>
 __global__ void __launch_bounds__(kThreads) alphaOnlyKernel(long long n, int integ, real* __restrict__ state,
                                                             const StepConst<real>* __restrict__ sc) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int order = kOrderDev(integ);
-    real u[5];
-    u[0] = state[i];
-    for (int s = 1; s <= order; ++s) {
-        real r = 0;
-        bool empty = true;
-        for (int k = 0; k < s; ++k) {
-            double a = kAlphaDev(integ, s - 1, k), b = kBetaDev(integ, s - 1, k);
-            if (a != 0) { real t = u[k] * (real)a; r = empty ? zfix(t) : r + t; empty = false; }
-            if (b != 0) { real t = (real)0. * sc->coef[s - 1][k]; r = empty ? zfix(t) : r + t; empty = false; }
-        }
-        u[s] = r;
-    }
-    state[i] = u[order];
+    state[i] = alphaOnlyElem<real>(integ, state[i], *sc);
 }
 
 template <typename real>
 __global__ void finalizeDtKernel(Phys<real> ph, int integ, int useFixed, double fixedDt, unsigned long long* acc,
                                  unsigned long long accInit, StepConst<real>* sc) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    real dt;
-    if (useFixed) dt = (real)fixedDt;
-    else {
-        real mn = (real)bitsToDouble(*acc, sizeof(real) == 4);
-        dt = (real)(mn * (real)ph.cfl);       // `return dt * app->cfl` with cfl a float
-        *acc = accInit;
-    }
-    sc->dt = dt;
-    sc->dt_f64 = (double)dt;
-    for (int s = 0; s < 3; ++s) sc->dt_dx[s] = dt / ph.dx[s];
-    for (int m = 0; m < 4; ++m)
-        for (int k = 0; k < 4; ++k) sc->coef[m][k] = (real)kBetaDev(integ, m, k) * dt;
+    finalizeOne<real>(ph, integ, useFixed, fixedDt, acc, accInit, sc);
 }
 
 __global__ void resetAccKernel(unsigned long long* acc, unsigned long long v) { *acc = v; }

@@ -1,0 +1,185 @@
+// hllc_cells.cuh -- per-cell bodies of the EulerHLLC kernels (res/EulerHLLC.cl),
+// shared by the single-problem kernels (hllc.cu) and the batched kernels (batch.cu).
+#pragma once
+#include "kernels.h"
+
+namespace hgpu {
+
+// state rotated so the normal momentum is component 1 (EulerHLLC.cl:32-47)
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void loadRotated(const real* __restrict__ s, long long c, real* out) {
+#pragma unroll
+    for (int j = 0; j < D + 2; ++j) out[j] = s[(long long)(D + 2) * c + j];
+    if (SIDE > 0) { real t = out[1]; out[1] = out[1 + SIDE]; out[1 + SIDE] = t; }
+}
+
+template <typename real, int D>
+struct Prim {
+    real density, invDensity, v[3], velocitySq, energyTotal, pressure, enthalpyTotal;
+};
+
+// primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238), potential 0.
+// `1. / densityL` and `(gamma - 1.) * ...` use double literals: FP32 promotes them.
+template <typename real, int D>
+__device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real, D>& p) {
+    const int E = D + 1;
+    p.density = st[0];
+    p.invDensity = (real)(1. / (double)p.density);
+    // VELOCITY: m/rho, by the correction step on RN(1/rho) in FP64 (fp64ops.cuh)
+#pragma unroll
+    for (int k = 0; k < D; ++k) p.v[k] = divByRecip(st[1 + k], p.density, p.invDensity);
+    p.velocitySq = p.v[0] * p.v[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + p.v[k] * p.v[k];
+    p.energyTotal = st[E] * p.invDensity;
+    real energyKinetic = halfOf(p.velocitySq);                          // .5f * velocitySq
+    real energyInternal = p.energyTotal - energyKinetic;
+    p.pressure = (real)(((double)gamma - 1.) * (double)p.density * (double)energyInternal);
+    p.enthalpyTotal = p.energyTotal + p.pressure * p.invDensity;
+}
+
+// sl, sr of one face (EulerHLLC.cl:85-97)
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, double gq, const real* __restrict__ state,
+                                         real* __restrict__ waves, long long c) {
+    real sL[D + 2], sR[D + 2];
+    loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
+    loadRotated<real, D, SIDE>(state, c, sR);
+    const double gm1 = (double)ph.gamma - 1.;
+    Prim<real, D> L, R;
+    primitives<real, D>(sL, ph.gamma, L);
+    primitives<real, D>(sR, ph.gamma, R);
+    real cL = (real)sqrt(gm1 * (double)(L.enthalpyTotal - halfOf(L.velocitySq)));
+    real cR = (real)sqrt(gm1 * (double)(R.enthalpyTotal - halfOf(R.velocitySq)));
+    // .5f * (pL + pR) - .5f * (vR - vL) * .5f * (rhoL + rhoR) * .5f * (cL + cR), halvings exact
+    real pressureStar = (real)fmaxLibm(0., (double)(halfOf(L.pressure + R.pressure) -
+                                                    halfOf(halfOf(halfOf(R.v[0] - L.v[0])) * (L.density + R.density)) *
+                                                        (cL + cR)));
+    real qL = pressureStar <= L.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / L.pressure) - 1.));
+    real qR = pressureStar <= R.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / R.pressure) - 1.));
+    waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - cL * qL;
+    waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + cR * qR;
+}
+
+// wave speeds of the faces of one cell: every axis in [2, S-2] (EulerHLLC.cl:110-131)
+template <typename real, int D>
+__device__ __forceinline__ void hllcWaveCell(const Grid& g, const Phys<real>& ph, double gq,
+                                             const real* __restrict__ state, real* __restrict__ waves, long long c,
+                                             int x, int y, int z) {
+    if (!inRange(g, x, y, z, 2, 1)) return;
+    waveFace<real, D, 0>(g, ph, gq, state, waves, c);
+    if (D > 1) waveFace<real, D, (D > 1 ? 1 : 0)>(g, ph, gq, state, waves, c);
+    if (D > 2) waveFace<real, D, (D > 2 ? 2 : 0)>(g, ph, gq, state, waves, c);
+}
+
+// cell timestep (EulerHLLC.cl:135-168): cells in [2, S-2], min over sides of
+// dx / (max(0, sr(face c)) - min(0, sl(face c+1))); INFINITY elsewhere
+template <typename real, int D>
+__device__ __forceinline__ unsigned long long hllcDtCell(const Grid& g, const Phys<real>& ph,
+                                                         const real* __restrict__ waves, long long c, int x, int y,
+                                                         int z, bool& nan) {
+    real result = (real)INFINITY;
+    if (inRange(g, x, y, z, 2, 1)) {
+#pragma unroll
+        for (int side = 0; side < D; ++side) {
+            real srHere = waves[((long long)side * 2 + 1) * g.V + c];
+            real slNext = waves[((long long)side * 2 + 0) * g.V + c + g.step[side]];
+            real minLambda = (real)fminLibm(0., (double)slNext);
+            real maxLambda = (real)fmaxLibm(0., (double)srHere);
+            real dum = ph.dx[side] / (maxLambda - minLambda);
+            if (dum != dum) nan = true;
+            result = fminLibm(result, dum);
+        }
+    }
+    return realBits(result);
+}
+
+// HLLC flux, HLLC_METHOD 2 (EulerHLLC.cl:240-418); `flux` holds the face's previous value.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
+                                         const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c) {
+    const int N = D + 2, E = N - 1;
+    real stL[N], stR[N];
+    loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
+    loadRotated<real, D, SIDE>(stage, c, stR);
+    Prim<real, D> L, R;
+    primitives<real, D>(stL, ph.gamma, L);
+    primitives<real, D>(stR, ph.gamma, R);
+    real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
+    real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
+    real fL[N], fR[N], flux[N];
+    fL[0] = L.density * L.v[0];
+    fL[1] = L.density * L.v[0] * L.v[0] + L.pressure;
+#pragma unroll
+    for (int k = 1; k < D; ++k) fL[1 + k] = L.density * L.v[k] * L.v[0];
+    fL[E] = L.density * L.enthalpyTotal * L.v[0];
+    fR[0] = R.density * R.v[0];
+    fR[1] = R.density * R.v[0] * R.v[0] + R.pressure;
+#pragma unroll
+    for (int k = 1; k < D; ++k) fR[1 + k] = R.density * R.v[k] * R.v[0];
+    fR[E] = R.density * R.enthalpyTotal * R.v[0];
+    real sStar = (R.density * R.v[0] * (sr - R.v[0]) - L.density * L.v[0] * (sl - L.v[0]) + L.pressure - R.pressure) /
+                 (R.density * (sr - R.v[0]) - L.density * (sl - L.v[0]));
+    bool taken = true;
+    if ((real)0. <= sl) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[i] = fL[i];
+    } else if (sl <= (real)0. && (real)0. <= sStar) {
+        real pressureLR = halfOf(L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
+                                 R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        // every component divides by (sl - sStar): one reciprocal, then exact corrected quotients
+        real den = sl - sStar, rden = (real)1. / den;
+        flux[0] = divByRecip(sStar * (sl * stL[0] - fL[0]), den, rden);
+        flux[1] = divByRecip(sStar * (sl * stL[1] - fL[1]) + sl * pressureLR, den, rden);
+#pragma unroll
+        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(sStar * (sl * stL[1 + k] - fL[1 + k]), den, rden);
+        flux[E] = divByRecip(sStar * (sl * stL[E] - fL[E]) + sl * pressureLR * sStar, den, rden);
+    } else if (sStar <= (real)0. && (real)0. <= sr) {
+        real pressureLR = halfOf(L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
+                                 R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        real den = sr - sStar, rden = (real)1. / den;
+        flux[0] = divByRecip(sStar * (sr * stR[0] - fR[0]), den, rden);
+        flux[1] = divByRecip(sStar * (sr * stR[1] - fR[1]) + sr * pressureLR, den, rden);
+#pragma unroll
+        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(sStar * (sr * stR[1 + k] - fR[1 + k]), den, rden);
+        flux[E] = divByRecip(sStar * (sr * stR[E] - fR[E]) + sr * pressureLR * sStar, den, rden);
+    } else if (sr <= (real)0.) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[i] = fR[i];
+    } else {
+        // no branch: the reference leaves the buffer's previous (global-frame) value,
+        // then applies the rotate-back swap to it
+        taken = false;
+#pragma unroll
+        for (int j = 0; j < N; ++j) flux[j] = fluxBuf[((long long)SIDE * N + j) * g.V + c];
+    }
+    if (SIDE > 0) { real t = flux[1]; flux[1] = flux[1 + SIDE]; flux[1 + SIDE] = t; }
+#pragma unroll
+    for (int j = 0; j < N; ++j) fluxBuf[((long long)SIDE * N + j) * g.V + c] = flux[j];
+    return taken;
+}
+
+// HLLC fluxes of the faces of one cell: along [2, S-2], transverse interior [2, S-3]
+// (the faces calcFluxDeriv reads).  Returns false if a face took no flux branch.
+template <typename real, int D>
+__device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
+                                             const real* __restrict__ waves, real* __restrict__ flux, long long c,
+                                             int x, int y, int z) {
+    bool ok = true;
+    int cc[3] = {x, y, z};
+#pragma unroll
+    for (int side = 0; side < D; ++side) {
+        bool in = true;
+        for (int a = 0; a < D; ++a) {
+            int hi = a == side ? 1 : 2;
+            if (cc[a] < 2 || cc[a] >= g.S[a] - hi) in = false;
+        }
+        if (!in) continue;
+        if (side == 0) ok &= hllcFace<real, D, 0>(g, ph, stage, waves, flux, c);
+        else if (side == 1) ok &= hllcFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
+        else ok &= hllcFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+    }
+    return ok;
+}
+
+}  // namespace hgpu

@@ -225,6 +225,41 @@ int hgpu_profile_update(hgpu_solver* s, int nsteps, hgpu_kernel_time* out, int c
 int hgpu_host_alloc(size_t bytes, void** ptr);
 int hgpu_host_free(void* ptr);
 
+/* ---- batches of independent problems ----
+ * No reference counterpart: the reference runs one problem per process
+ * (src/HydroGPUApp.cpp:330-349).  A batch holds problems of the same solver, dim,
+ * integrator, limiter, precision and use_fixed_dt, each with its own size, domain,
+ * gamma, cfl, boundary methods and dt; every step of all of them is one CUDA graph of
+ * persistent launches that pull work tiles from an atomic queue.  Each problem's
+ * result is bit-identical to running it alone with hgpu_update. */
+typedef struct hgpu_batch hgpu_batch;
+
+typedef struct hgpu_batch_tuning {
+    int tile_x, tile_y, tile_z;   /* cells per work tile (product <= 256)            */
+    int staged;                   /* Roe eigenbasis: per-cell values via shared memory */
+    int blocks_per_sm;            /* persistent blocks per SM, 0 = occupancy limit     */
+} hgpu_batch_tuning;
+
+int hgpu_batch_create(const hgpu_config* cfgs, int nproblems, hgpu_batch** out);
+int hgpu_batch_destroy(hgpu_batch* b);
+int hgpu_batch_info(const hgpu_batch* b, int* nproblems, long long* total_cells, int* kernels_per_step);
+/* Upload / download problem p's full state (AoS, ghosts included). */
+int hgpu_batch_set_state(hgpu_batch* b, int problem, const void* host_state, size_t count);
+int hgpu_batch_get_state(hgpu_batch* b, int problem, void* host_state, size_t count);
+/* Advance every problem nsteps Solver::update steps (graph replays; returns when queued). */
+int hgpu_batch_update(hgpu_batch* b, int nsteps);
+/* Same, returning the device time of the nsteps in milliseconds (CUDA events). */
+int hgpu_batch_timed_update(hgpu_batch* b, int nsteps, float* ms);
+/* dt of the most recent step of every problem (n = number of problems). */
+int hgpu_batch_dts(hgpu_batch* b, double* dts, int n);
+int hgpu_batch_health(hgpu_batch* b, uint32_t* flags);
+int hgpu_batch_get_tuning(const hgpu_batch* b, hgpu_batch_tuning* t);
+int hgpu_batch_set_tuning(hgpu_batch* b, const hgpu_batch_tuning* t);
+/* Time candidate tunings for `steps` steps each on this batch (its state is restored
+ * afterwards) and keep the fastest; with a cache file the result is looked up first
+ * and appended after tuning, keyed by the batch's shape. */
+int hgpu_batch_autotune(hgpu_batch* b, const char* cache_path, int steps);
+
 /* CFL timestep of a ghost-filled device state without allocating device memory.
  * No counterpart in the reference: it is for callers that cannot call cudaMalloc
  * (hosts that own the whole device-memory budget through their own pool, code that

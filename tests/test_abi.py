@@ -1,5 +1,6 @@
 """The C ABI library: loads without a GPU, exports every declared entry point, and
 its host-only calls work; compute calls fail loudly when no GPU is present."""
+import ctypes
 import os
 import re
 
@@ -71,3 +72,22 @@ def _has_gpu():
 def test_no_silent_cpu_fallback(hg):
     with pytest.raises(hgmod.HgpuError):
         hgmod.Solver(size=(16, 16))
+
+
+def test_batch_rejects_mixed_configs(hg):
+    """Batch validation runs before any device work: mixed solvers, dims or
+    integrators and the SEAM scheme are refused with a status code."""
+    codes = {v: k for k, v in _abi.STATUS_NAMES.items()}
+    a = _abi.make_config(solver="EulerRoe", size=(20, 20))
+    for other in (_abi.make_config(solver="EulerHLLC", size=(20, 20)),
+                  _abi.make_config(solver="EulerRoe", size=(20, 20), integrator="RungeKutta4"),
+                  _abi.make_config(solver="EulerRoe", size=(20,))):
+        arr = (_abi.HgpuConfig * 2)(a, other)
+        h = ctypes.c_void_p()
+        assert hg.lib().hgpu_batch_create(arr, 2, ctypes.byref(h)) == codes["HGPU_ERR_CONFIG"]
+        assert not h.value
+    seam = _abi.make_config(solver="EulerRoe", size=(20, 20), compat=_abi.COMPAT_SEAM)
+    arr = (_abi.HgpuConfig * 1)(seam)
+    h = ctypes.c_void_p()
+    assert hg.lib().hgpu_batch_create(arr, 1, ctypes.byref(h)) == codes["HGPU_ERR_UNSUPPORTED"]
+    assert hg.lib().hgpu_batch_create(arr, 0, ctypes.byref(h)) == codes["HGPU_ERR_ARG"]
