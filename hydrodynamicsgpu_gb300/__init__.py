@@ -46,6 +46,14 @@ SIGNATURES = {
     "hgpu_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "hgpu_host_free": (ctypes.c_int, [_P]),
     "hgpu_cfl_timestep_noalloc": (ctypes.c_int, [_CFG, _P, ctypes.POINTER(ctypes.c_double), _P]),
+    "hgpu_update_frozen_dt": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_double]),
+    "hgpu_checkpoint_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "hgpu_checkpoint_forward": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_checkpoint_dts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "hgpu_checkpoint_backward": (ctypes.c_int, [_P, _P, _P]),
+    "hgpu_checkpoint_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "hgpu_checkpoint_destroy": (ctypes.c_int, [_P]),
     "hgpu_batch_create": (ctypes.c_int, [_CFG, ctypes.c_int, ctypes.POINTER(_P)]),
     "hgpu_batch_destroy": (ctypes.c_int, [_P]),
     "hgpu_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
@@ -243,6 +251,19 @@ class Solver:
         check(lib().hgpu_stream(self.h, ctypes.byref(p)))
         return p.value
 
+    def update_frozen_dt(self, dts):
+        """Advance len(dts) steps with the given dt per step (eigenbasis and stages as
+        in update(), the CFL reduction replaced by the given value)."""
+        a = np.ascontiguousarray(dts, dtype=np.float64)
+        check(lib().hgpu_update_frozen_dt(self.h, a.size, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        self.frame += a.size
+
+    def adjoint_step(self, d_u, d_lam_next, d_lam_out, dt):
+        """lam_out = (d u^{n+1}/d u^n)^T lam_next for the step from u^n with dt; device
+        pointers (ints) to full FP64 state arrays."""
+        check(lib().hgpu_adjoint_step(self.h, ctypes.c_void_p(d_u), ctypes.c_void_p(d_lam_next),
+                                      ctypes.c_void_p(d_lam_out), float(dt)))
+
     def save(self, prefix):
         """Solver::save (src/Solver/Solver.cpp:563-589) without the FITS dependency:
         one little-endian raw file per state channel, <prefix><STATE>.raw, plus
@@ -334,3 +355,47 @@ class Batch:
     def autotune(self, cache_path=None, steps=2):
         check(lib().hgpu_batch_autotune(self.h, cache_path.encode() if cache_path else None, int(steps)))
         return self.tuning()
+
+
+class Checkpoints:
+    """Checkpointed trajectory of `nsteps` steps from the solver's current state
+    (hgpu_checkpoint_*): forward() keeps every `every`-th state and each step's dt,
+    backward() maps the cotangent of the final state to that of the initial state."""
+
+    def __init__(self, solver, nsteps, every):
+        h = ctypes.c_void_p()
+        check(lib().hgpu_checkpoint_create(solver.h, int(nsteps), int(every), ctypes.byref(h)))
+        self.h, self.solver, self.nsteps = h, solver, int(nsteps)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hgpu_checkpoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, dts=None):
+        if dts is None:
+            check(lib().hgpu_checkpoint_forward(self.h, None))
+        else:
+            a = np.ascontiguousarray(dts, dtype=np.float64)
+            if a.size != self.nsteps:
+                raise ValueError("need %d dt values" % self.nsteps)
+            check(lib().hgpu_checkpoint_forward(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+
+    def dts(self):
+        out = (ctypes.c_double * self.nsteps)()
+        check(lib().hgpu_checkpoint_dts(self.h, out, self.nsteps))
+        return np.array(out[:])
+
+    def backward(self, d_lam_T, d_lam_0):
+        check(lib().hgpu_checkpoint_backward(self.h, ctypes.c_void_p(d_lam_T), ctypes.c_void_p(d_lam_0)))
+
+    def times(self):
+        f, b = ctypes.c_float(), ctypes.c_float()
+        check(lib().hgpu_checkpoint_times(self.h, ctypes.byref(f), ctypes.byref(b)))
+        return f.value, b.value

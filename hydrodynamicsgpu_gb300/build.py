@@ -26,12 +26,15 @@ SOURCES = {
     "kernels/probe.cu": [],
     "kernels/noalloc.cu": ["--fmad=false"],
     "kernels/batch.cu": ["--fmad=false"],
+    "kernels/adjoint.cu": [],
+    "host/adjoint.cu": [],
     "host/batch_solver.cu": [],
     "host/solver.cu": [],
     "host/capi.cu": [],
 }
 HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
-           "kernels/combine_cells.cuh", "kernels/batch.h", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h"]
+           "kernels/combine_cells.cuh", "kernels/batch.h", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",
+           "kernels/adjoint.h", "host/adjoint.h"]
 
 
 def nvcc():

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint.h"
 #include "batch_solver.h"
 #include "solver.h"
 
@@ -20,6 +21,12 @@ struct hgpu_solver {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int kernelsPerStep = 0;
+    std::unique_ptr<hgpu::RoeAdjoint> adjoint;   // created on first use
+};
+
+struct hgpu_checkpoint {
+    hgpu_solver* h;
+    std::unique_ptr<hgpu::Checkpoints> c;
 };
 
 namespace {
@@ -300,6 +307,87 @@ int hgpu_host_alloc(size_t bytes, void** ptr) {
 int hgpu_host_free(void* ptr) {
     return guarded([&]() {
         if (ptr) hgpu::cudaCheck(cudaFreeHost(ptr), "cudaFreeHost");
+        return (int)HGPU_OK;
+    });
+}
+
+namespace {
+hgpu::RoeAdjoint& adjointOf(hgpu_solver* h) {
+    if (!h->adjoint) {
+        auto* s = dynamic_cast<hgpu::Solver<double>*>(h->s.get());
+        if (!s) throw hgpu::ConfigError(HGPU_ERR_UNSUPPORTED, "the adjoint covers EulerRoe in FP64");
+        h->adjoint.reset(new hgpu::RoeAdjoint(s->rc, s->stream));
+    }
+    return *h->adjoint;
+}
+}  // namespace
+
+int hgpu_update_frozen_dt(hgpu_solver* h, int nsteps, const double* dts) {
+    if (!h || nsteps < 0 || (nsteps > 0 && !dts)) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        hgpu::RoeAdjoint& a = adjointOf(h);
+        double* st = static_cast<double*>(h->s->stateDevicePtr());
+        for (int i = 0; i < nsteps; ++i) a.advance(st, dts[i]);
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_adjoint_step(hgpu_solver* h, const void* d_u_n, const void* d_lambda_next, void* d_lambda_n, double dt) {
+    if (!h || !d_u_n || !d_lambda_next || !d_lambda_n) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        adjointOf(h).step(static_cast<const double*>(d_u_n), static_cast<const double*>(d_lambda_next),
+                          static_cast<double*>(d_lambda_n), dt);
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoint** out) {
+    if (!h || !out || nsteps < 1 || every < 1) return fail(HGPU_ERR_ARG, "bad argument");
+    *out = nullptr;
+    return guarded([&]() {
+        hgpu::RoeAdjoint& a = adjointOf(h);
+        auto* s = dynamic_cast<hgpu::Solver<double>*>(h->s.get());
+        std::unique_ptr<hgpu_checkpoint> c(new hgpu_checkpoint());
+        c->h = h;
+        c->c.reset(new hgpu::Checkpoints(&a, s->state.as<double>(), s->stream, nsteps, every,
+                                         [h]() { runSteps(h, 1); }, &s->sc()->dt_f64));
+        *out = c.release();
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_checkpoint_forward(hgpu_checkpoint* c, const double* dts) {
+    if (!c) return fail(HGPU_ERR_ARG, "null handle");
+    return guarded([&]() { c->c->forward(dts); return (int)HGPU_OK; });
+}
+
+int hgpu_checkpoint_dts(hgpu_checkpoint* c, double* dts, int n) {
+    if (!c || !dts) return fail(HGPU_ERR_ARG, "null argument");
+    if (n != (int)c->c->dts.size()) return fail(HGPU_ERR_ARG, "dt array size mismatch");
+    std::copy(c->c->dts.begin(), c->c->dts.end(), dts);
+    return HGPU_OK;
+}
+
+int hgpu_checkpoint_backward(hgpu_checkpoint* c, const void* d_lambda_T, void* d_lambda_0) {
+    if (!c || !d_lambda_T || !d_lambda_0) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        c->c->backward(static_cast<const double*>(d_lambda_T), static_cast<double*>(d_lambda_0));
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_checkpoint_times(hgpu_checkpoint* c, float* forward_ms, float* backward_ms) {
+    if (!c) return fail(HGPU_ERR_ARG, "null handle");
+    if (forward_ms) *forward_ms = c->c->forwardMs;
+    if (backward_ms) *backward_ms = c->c->backwardMs;
+    return HGPU_OK;
+}
+
+int hgpu_checkpoint_destroy(hgpu_checkpoint* c) {
+    if (!c) return HGPU_OK;
+    return guarded([&]() {
+        cudaStreamSynchronize(c->h->s->stream);
+        delete c;
         return (int)HGPU_OK;
     });
 }

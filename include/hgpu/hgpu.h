@@ -260,6 +260,36 @@ int hgpu_batch_set_tuning(hgpu_batch* b, const hgpu_batch_tuning* t);
  * and appended after tuning, keyed by the batch's shape. */
 int hgpu_batch_autotune(hgpu_batch* b, const char* cache_path, int steps);
 
+/* ---- differentiation (EulerRoe, FP64, REF scheme) ----
+ * No reference counterpart: the reference runs the forward scheme only
+ * (src/Solver/Roe.cpp:82-112).  The differentiated step is Solver::update with dt
+ * held at a given value ("frozen"): ghost fill, eigenbasis of u^n, the integrator's
+ * stages.  With the dt the CFL condition chose, the frozen step is bit-identical to
+ * hgpu_update's step. */
+
+/* Advance nsteps steps with the given dt per step (host array of nsteps values). */
+int hgpu_update_frozen_dt(hgpu_solver* h, int nsteps, const double* dts);
+
+/* One vector-Jacobian product: lambda_n = (d u^{n+1} / d u^n)^T lambda_next for the
+ * step from u_n with dt.  All three are DEVICE arrays of the full state (AoS, ghosts
+ * included); lambda_n must not alias lambda_next.  Runs on the solver's stream and
+ * returns when queued; the solver's own state is not touched. */
+int hgpu_adjoint_step(hgpu_solver* h, const void* d_u_n, const void* d_lambda_next, void* d_lambda_n, double dt);
+
+/* Checkpointed trajectory of nsteps steps from the solver's current state: the
+ * forward keeps the state every `every` steps (and each step's dt), the backward
+ * recomputes one segment at a time and runs its reverse steps. */
+typedef struct hgpu_checkpoint hgpu_checkpoint;
+int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoint** out);
+/* dts: nsteps frozen values, or NULL for the CFL dt of each step (recorded). */
+int hgpu_checkpoint_forward(hgpu_checkpoint* c, const double* dts);
+int hgpu_checkpoint_dts(hgpu_checkpoint* c, double* dts, int n);
+/* lambda_0 = (d u^T / d u^0)^T lambda_T; DEVICE arrays of the full state. */
+int hgpu_checkpoint_backward(hgpu_checkpoint* c, const void* d_lambda_T, void* d_lambda_0);
+/* device time of the last forward and backward (CUDA events on the solver stream) */
+int hgpu_checkpoint_times(hgpu_checkpoint* c, float* forward_ms, float* backward_ms);
+int hgpu_checkpoint_destroy(hgpu_checkpoint* c);
+
 /* CFL timestep of a ghost-filled device state without allocating device memory.
  * No counterpart in the reference: it is for callers that cannot call cudaMalloc
  * (hosts that own the whole device-memory budget through their own pool, code that
