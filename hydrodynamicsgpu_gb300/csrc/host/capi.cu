@@ -1,6 +1,7 @@
 // capi.cu -- the extern "C" boundary declared in include/hgpu/hgpu.h.
 // No C++ exception crosses it: every entry point maps failures to an hgpu_status
 // and keeps a per-thread message for hgpu_last_error().
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -22,6 +23,7 @@ struct hgpu_solver {
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int kernelsPerStep = 0;
     std::unique_ptr<hgpu::RoeAdjoint> adjoint;   // created on first use
+    std::vector<hgpu_checkpoint*> checkpoints;   // live trajectories of this solver
 };
 
 struct hgpu_checkpoint {
@@ -145,6 +147,10 @@ int hgpu_destroy(hgpu_solver* h) {
     if (!h) return HGPU_OK;
     return guarded([&]() {
         if (h->s && h->s->stream) cudaStreamSynchronize(h->s->stream);
+        for (hgpu_checkpoint* c : h->checkpoints) {   // they keep pointers into this solver
+            c->c.reset();
+            c->h = nullptr;
+        }
         destroyGraph(h);
         if (h->t0) cudaEventDestroy(h->t0);
         if (h->t1) cudaEventDestroy(h->t1);
@@ -351,6 +357,7 @@ int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoin
         c->h = h;
         c->c.reset(new hgpu::Checkpoints(&a, s->state.as<double>(), s->stream, nsteps, every,
                                          [h]() { runSteps(h, 1); }, &s->sc()->dt_f64));
+        h->checkpoints.push_back(c.get());
         *out = c.release();
         return (int)HGPU_OK;
     });
@@ -358,11 +365,13 @@ int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoin
 
 int hgpu_checkpoint_forward(hgpu_checkpoint* c, const double* dts) {
     if (!c) return fail(HGPU_ERR_ARG, "null handle");
+    if (!c->c) return fail(HGPU_ERR_ARG, "the solver of this checkpoint was destroyed");
     return guarded([&]() { c->c->forward(dts); return (int)HGPU_OK; });
 }
 
 int hgpu_checkpoint_dts(hgpu_checkpoint* c, double* dts, int n) {
     if (!c || !dts) return fail(HGPU_ERR_ARG, "null argument");
+    if (!c->c) return fail(HGPU_ERR_ARG, "the solver of this checkpoint was destroyed");
     if (n != (int)c->c->dts.size()) return fail(HGPU_ERR_ARG, "dt array size mismatch");
     std::copy(c->c->dts.begin(), c->c->dts.end(), dts);
     return HGPU_OK;
@@ -370,6 +379,7 @@ int hgpu_checkpoint_dts(hgpu_checkpoint* c, double* dts, int n) {
 
 int hgpu_checkpoint_backward(hgpu_checkpoint* c, const void* d_lambda_T, void* d_lambda_0) {
     if (!c || !d_lambda_T || !d_lambda_0) return fail(HGPU_ERR_ARG, "null argument");
+    if (!c->c) return fail(HGPU_ERR_ARG, "the solver of this checkpoint was destroyed");
     return guarded([&]() {
         c->c->backward(static_cast<const double*>(d_lambda_T), static_cast<double*>(d_lambda_0));
         return (int)HGPU_OK;
@@ -378,6 +388,7 @@ int hgpu_checkpoint_backward(hgpu_checkpoint* c, const void* d_lambda_T, void* d
 
 int hgpu_checkpoint_times(hgpu_checkpoint* c, float* forward_ms, float* backward_ms) {
     if (!c) return fail(HGPU_ERR_ARG, "null handle");
+    if (!c->c) return fail(HGPU_ERR_ARG, "the solver of this checkpoint was destroyed");
     if (forward_ms) *forward_ms = c->c->forwardMs;
     if (backward_ms) *backward_ms = c->c->backwardMs;
     return HGPU_OK;
@@ -386,7 +397,11 @@ int hgpu_checkpoint_times(hgpu_checkpoint* c, float* forward_ms, float* backward
 int hgpu_checkpoint_destroy(hgpu_checkpoint* c) {
     if (!c) return HGPU_OK;
     return guarded([&]() {
-        cudaStreamSynchronize(c->h->s->stream);
+        if (c->h) {
+            cudaStreamSynchronize(c->h->s->stream);
+            auto& v = c->h->checkpoints;
+            v.erase(std::remove(v.begin(), v.end(), c), v.end());
+        }
         delete c;
         return (int)HGPU_OK;
     });

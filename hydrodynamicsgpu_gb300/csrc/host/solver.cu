@@ -24,7 +24,12 @@ DeviceBuffer::DeviceBuffer(size_t bytes, bool zero) : bytes_(bytes) {
         (void)cudaGetLastError();
         throw CudaError(e, "cudaMalloc of " + std::to_string(bytes) + " bytes");
     }
-    if (zero) cudaCheck(cudaMemset(ptr_, 0, bytes), "cudaMemset");
+    if (zero) {
+        // the memset runs on the legacy stream, which the solvers' non-blocking streams
+        // do not wait for: finish it before any kernel can read the buffer
+        cudaCheck(cudaMemset(ptr_, 0, bytes), "cudaMemset");
+        cudaCheck(cudaStreamSynchronize(nullptr), "cudaMemset sync");
+    }
 }
 
 DeviceBuffer::~DeviceBuffer() {

@@ -61,12 +61,14 @@ __device__ __forceinline__ float fmaxLibm(float x, float y) { return (x > y || y
 // (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
 // processor", IBM J. Res. Dev. 34(1), 1990; checked here against the hardware
 // division on 3.8e9 random and near-midpoint operand pairs, none differing).
-// Zeros take their IEEE sign; operands outside a safe exponent window (subnormal,
-// huge, Inf, NaN) take the hardware division, so q' and r never leave the normal range.
+// A zero x over a finite nonzero b gives the zero of sign(x) xor sign(b); operands
+// outside a safe exponent window (zero, subnormal, huge, Inf, NaN -- so 0/0 and x/0
+// too) take the hardware division, so q' and r never leave the normal range.
 __device__ __forceinline__ double divByRecip(double x, double b, double rb) {
     long long bx = bitsOf(x), bb = bitsOf(b);
     int ex = (int)((bx >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
-    if ((bx & 0x7FFFFFFFFFFFFFFFLL) == 0) return fromBits((bx ^ bb) & (long long)0x8000000000000000ULL);
+    if ((bx & 0x7FFFFFFFFFFFFFFFLL) == 0 && eb != 0 && eb != 0x7FF)
+        return fromBits((bx ^ bb) & (long long)0x8000000000000000ULL);
     if (ex < 623 || ex > 1423 || eb < 623 || eb > 1423) return x / b;
     double q = x * rb;
     double r = fma(-b, q, x);

@@ -2,8 +2,8 @@
 
 Checked three ways: against the gradient of the pure-torch restatement
 (tests/torch_euler.py, autograd; agreement to 1e-10 relative), against central
-finite differences of the CUDA forward with dt frozen (eps 1e-6, agreement
-1e-6 relative), and the checkpointed trajectory against a chain of single-step
+finite differences of the CUDA forward with dt frozen (eps 1e-6 along unit
+random directions, agreement 1e-6 relative), and the checkpointed trajectory against a chain of single-step
 products (identical bits for every checkpoint interval)."""
 import numpy as np
 import pytest
@@ -92,7 +92,8 @@ CASES = [
     (2, "MIRROR", "RungeKutta3TVD", "Superbee"),
     (2, "FREEFLOW", "RungeKutta2Heun", "MonotizedCentral"),
     (2, "PERIODIC", "RungeKutta4", "Koren"),
-    (2, [("PERIODIC", "PERIODIC"), ("MIRROR", "FREEFLOW")], "RungeKutta2", "VanAlbada1"),
+    (2, [("PERIODIC", "PERIODIC"), ("MIRROR", "FREEFLOW")], "RungeKutta2", "MinMod"),
+    (2, "PERIODIC", "RungeKutta2", "VanAlbada1"),
     (3, "MIRROR", "RungeKutta2", "Superbee"),
     (3, "PERIODIC", "RungeKutta4", "MinMod"),
 ]
@@ -120,7 +121,8 @@ def test_adjoint_step_matches_finite_differences(hg, dim, bnd, integ, lim):
     dt = cfl_dt(hg, cfg, u)
     g = gpu_vjp(hg, cfg, u, lam, dt)
     for _ in range(4):
-        d = rng.standard_normal(u.size) * np.abs(u)
+        d = rng.standard_normal(u.size)
+        d /= np.linalg.norm(d)                # unit direction
         fp = gpu_frozen(hg, cfg, u + FD_EPS * d, [dt])
         fm = gpu_frozen(hg, cfg, u - FD_EPS * d, [dt])
         fd = float(np.dot(lam, fp - fm)) / (2 * FD_EPS)
@@ -142,10 +144,10 @@ def test_frozen_dt_step_is_the_cfl_step(hg):
         a.close()
 
 
-def kh_small(n=24, seed=100):
+def kh_small(n=24, seed=100, limiter="MinMod"):
     size = (n + 4, n + 4)
     st = ic.kelvin_helmholtz(size=size, seed=seed)
-    return _abi.make_config(solver="EulerRoe", size=size, boundary="PERIODIC", limiter="MinMod",
+    return _abi.make_config(solver="EulerRoe", size=size, boundary="PERIODIC", limiter=limiter,
                             integrator="RungeKutta2"), st.reshape(-1)
 
 
@@ -198,8 +200,22 @@ def test_checkpointed_gradient(hg, oracle_mod, every):
     s.close()
 
 
+def drifting_flow(n=32, limiter="VanAlbada1"):
+    """Smooth periodic flow whose velocities stay away from zero (u ~ .4, v ~ .3):
+    no face changes its upwind side and VanAlbada1 has no kinks, so the rollout is
+    differentiable and central differences converge to the adjoint."""
+    size = (n + 4, n + 4)
+    f = [ic.smooth_perturbation(size, seed=400 + k, amp=1.)[0] for k in range(4)]
+    st = ic.build_state_euler(2, 1.4, 1. + .2 * f[0], .4 + .05 * f[1], .3 + .05 * f[2], 0., 1. + .1 * f[3])
+    return _abi.make_config(solver="EulerRoe", size=size, boundary="PERIODIC", limiter=limiter,
+                            integrator="RungeKutta2"), st.reshape(-1)
+
+
 def test_checkpointed_gradient_vs_finite_differences(hg):
-    cfg, u0 = kh_small(n=32, seed=101)
+    """40 steps of a smooth drifting flow.  (On the Kelvin-Helmholtz state the normal
+    velocity of many faces is within the noise of zero, so perturbations switch their
+    upwind side -- a kink -- and the difference quotient is not a derivative.)"""
+    cfg, u0 = drifting_flow()
     nsteps = 40
     s = hg.Solver(cfg)
     s.resetState(u0)
@@ -220,7 +236,8 @@ def test_checkpointed_gradient_vs_finite_differences(hg):
     g = out.cpu().numpy()
     rng = np.random.default_rng(300)
     for _ in range(4):
-        d = rng.standard_normal(u0.size) * np.abs(u0)
+        d = rng.standard_normal(u0.size)
+        d /= np.linalg.norm(d)
         lp, _ = density_loss_cotangent(cfg, gpu_frozen(hg, cfg, u0 + FD_EPS * d, dts), target)
         lm, _ = density_loss_cotangent(cfg, gpu_frozen(hg, cfg, u0 - FD_EPS * d, dts), target)
         fd = (lp - lm) / (2 * FD_EPS)

@@ -37,12 +37,13 @@ def tableau(integrator):
 
 
 def _mn(a, b):
-    """C library fmin: a NaN operand yields the other one."""
-    return torch.where(torch.isnan(b), a, torch.where(torch.isnan(a), b, torch.minimum(a, b)))
+    """fmin as the kernels and the oracle evaluate it: a NaN operand yields the other
+    one, ties yield the second; the derivative is that of the operand selected."""
+    return torch.where(torch.isnan(b), a, torch.where(torch.isnan(a), b, torch.where(a < b, a, b)))
 
 
 def _mx(a, b):
-    return torch.where(torch.isnan(b), a, torch.where(torch.isnan(a), b, torch.maximum(a, b)))
+    return torch.where(torch.isnan(b), a, torch.where(torch.isnan(a), b, torch.where(a > b, a, b)))
 
 
 def _limiter(name, r):
@@ -214,7 +215,11 @@ def derivative(u, basis, dim, dx, dt, limiter):
         safe = torch.where(mask & ~zero, dq, torch.ones_like(dq))
         dqUp = torch.where(up, dqM, dqP)
         r = torch.where(zero, (dqUp / dq).detach(), dqUp / safe)
-        phi = _limiter(limiter, r)
+        # limiter of non-finite r: value only (no derivative leaks through masked faces)
+        fin = torch.isfinite(r)
+        phi = torch.where(fin, _limiter(limiter, torch.where(fin, r, torch.zeros_like(r))),
+                          _limiter(limiter, r).detach())
+        phi = torch.where(mask, phi, torch.zeros_like(phi))   # unused there; keeps 0 * NaN out of R's cotangent
         eps = lam * (dt / dx[side])
         ft = ft - .5 * lam * dq * (theta + phi * (eps - theta))
         F = torch.einsum("...ij,...j->...i", R, ft)
