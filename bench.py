@@ -44,6 +44,13 @@ def parse():
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batched sweep")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
+    ap.add_argument("--batch-problems", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--adjoint-problems", type=int, default=16)
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--fd-directions", type=int, default=64)
     return ap.parse_args()
 
 
@@ -211,6 +218,200 @@ def algorithmic_bytes_per_cell(kind):
     return table.get(kind, 0)
 
 
+def batched_sweep(hg, _abi, ic, args):
+    """The batched workload: 512 four-quadrant Riemann problems of uneven sides
+    (16*round(exp(U(ln 32, ln 512))/16) cells per axis, ghosts included, seed 2),
+    EulerRoe FP64, RK2 midpoint, Superbee, CFL 0.5, periodic or free-flow per problem.
+    Timed three ways over the same steps: one batched CUDA graph of persistent
+    launches per step; per-problem plain launches issued problem after problem (each
+    problem's steps, then the next problem, as a sweep of the single-problem solver
+    runs); and per-problem plain launches interleaved step by step, each problem on
+    its own stream."""
+    cfgs, inits = [], []
+    for pr in ic.random_quadrant_problems(n=args.batch_problems, seed=2):
+        side = pr["side"]
+        cfgs.append(_abi.make_config(solver="EulerRoe", size=(side, side), boundary=pr["boundary"],
+                                     limiter="Superbee", integrator="RungeKutta2"))
+        inits.append(ic.quadrant((side, side), pr["quadrants"]).reshape(-1))
+    interior = sum((c.size[0] - 4) * (c.size[1] - 4) for c in cfgs)
+    steps = args.batch_steps
+    b = hg.Batch(cfgs)
+    for p, x in enumerate(inits):
+        b.set_state(p, x)
+    t0 = time.perf_counter()
+    tuning = b.autotune(os.path.join(REPO, "hydrodynamicsgpu_gb300", ".batch_tuning.txt"), steps=2)
+    tune_s = time.perf_counter() - t0
+    for p, x in enumerate(inits):
+        b.set_state(p, x)
+    b.update(3)
+    batch_ms = b.timed_update(steps) / steps
+    _, total_cells, kps = b.info()
+    health = b.health()
+    b.close()
+    solvers = [hg.Solver(c) for c in cfgs]
+    for s_, x in zip(solvers, inits):
+        s_.resetState(x)
+        s_.update(2, want_dt=False)
+    for s_ in solvers:
+        s_.synchronize()
+    t0 = time.perf_counter()
+    for s_ in solvers:
+        s_.update(steps, want_dt=False)
+        s_.synchronize()
+    seq_ms = (time.perf_counter() - t0) * 1e3 / steps
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s_ in solvers:
+            s_.update(1, want_dt=False)
+    for s_ in solvers:
+        s_.synchronize()
+    inter_ms = (time.perf_counter() - t0) * 1e3 / steps
+    for s_ in solvers:
+        s_.close()
+    rate = lambda ms: interior / (ms * 1e-3)
+    return {
+        "workload": "%d four-quadrant Riemann problems, sides 32-512 (seed 2), EulerRoe RK2 Superbee FP64"
+                    % len(cfgs),
+        "interior_cells": interior, "steps": steps,
+        "batched": {"value": rate(batch_ms), "ms_per_step": batch_ms, "kernels_per_step": kps,
+                    "tuning": {"tile": list(tuning[:3]), "staged_eigenbasis": tuning[3],
+                               "blocks_per_sm": tuning[4]}, "autotune_s": tune_s, "health_flags": health},
+        "plain_sequential": {"value": rate(seq_ms), "ms_per_step": seq_ms},
+        "plain_interleaved": {"value": rate(inter_ms), "ms_per_step": inter_ms},
+        "speedup_vs_plain_sequential": seq_ms / batch_ms,
+        "speedup_vs_plain_interleaved": inter_ms / batch_ms,
+        "unit": UNIT, "timing": "batched: CUDA events; plain: host wall clock around the launches + synchronize",
+    }
+
+
+def smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, pert, ndir=8):
+    """The same gradient check on a configuration where the rollout is differentiable:
+    a smooth periodic flow with velocities away from zero (no face switches its upwind
+    side) and the smooth VanAlbada1 limiter, 512^2, RK2, the same step count."""
+    import torch
+    f = [ic.smooth_perturbation((n, n), seed=400 + k, amp=1.)[0] for k in range(4)]
+    u0 = ic.build_state_euler(2, 1.4, 1. + .2 * f[0], .4 + .05 * f[1], .3 + .05 * f[2], 0.,
+                              1. + .1 * f[3]).reshape(-1)
+    cfg = _abi.make_config(solver="EulerRoe", size=(n, n), boundary="PERIODIC", limiter="VanAlbada1",
+                           integrator="RungeKutta2")
+    s_ = hg.Solver(cfg)
+    s_.resetState(u0)
+    cp = hg.Checkpoints(s_, args.adjoint_steps, 20)
+    cp.forward()
+    dts = cp.dts()
+    uT = s_.getState().copy()
+    target = uT.reshape(n, n, N_STATES)[..., 0] + pert
+    _, lamT = loss_and_cotangent(uT, target)
+    dl = torch.tensor(lamT, device="cuda")
+    g = torch.empty_like(dl)
+    torch.cuda.synchronize()
+    cp.backward(dl.data_ptr(), g.data_ptr())
+    s_.synchronize()
+    gh = g.cpu().numpy()
+    rng = np.random.default_rng(300)
+    errs = []
+    for _ in range(ndir):
+        d = rng.standard_normal(u0.size)
+        d /= np.linalg.norm(d)
+        vals = []
+        for sgn in (1, -1):
+            s_.resetState(u0 + sgn * 1e-6 * d)
+            s_.update_frozen_dt(dts)
+            vals.append(loss_and_cotangent(s_.getState(), target)[0])
+        ad = float(np.dot(gh, d))
+        errs.append(abs((vals[0] - vals[1]) / 2e-6 - ad) / abs(ad))
+    cp.close()
+    s_.close()
+    errs = np.array(errs)
+    return {"workload": "smooth drifting flow 512^2, VanAlbada1, RK2, %d steps" % args.adjoint_steps,
+            "directions": ndir, "eps": 1e-6, "rel_err_median": float(np.median(errs)),
+            "rel_err_max": float(errs.max()), "within_1e-6": int((errs <= 1e-6).sum())}
+
+
+def adjoint_measure(hg, _abi, ic, args):
+    """Adjoint workload: Kelvin-Helmholtz 512^2 problems (seeds 100..), EulerRoe FP64
+    RK2 MinMod periodic, `adjoint_steps` steps with CFL dt recorded and then frozen,
+    checkpoints every 20 steps.  forward = checkpointed forward; backward = segment
+    recompute + reverse steps.  Loss = mean over interior cells of
+    (rho_T - rho_target)^2 with rho_target = rho_T + a smooth 1e-2 perturbation
+    (seed 200).  Central differences (eps 1e-6, unit random directions, seed 300) of
+    the frozen-dt forward check the gradient of problem 0."""
+    import torch
+    n = 512
+    shape = (n, n, N_STATES)
+    mask = np.zeros((n, n), dtype=bool)
+    mask[2:-2, 2:-2] = True
+    pert = ic.smooth_perturbation((n, n), seed=200)[0]
+
+    def loss_and_cotangent(uT, target):
+        r = uT.reshape(shape)[..., 0] - target
+        cnt = mask.sum()
+        lam = np.zeros(shape)
+        lam[..., 0][mask] = 2 * r[mask] / cnt
+        return float(np.sum(r[mask] ** 2) / cnt), lam.reshape(-1)
+
+    fwd_ms = bwd_ms = plain_ms = 0.
+    fd = None
+    for k in range(args.adjoint_problems):
+        cfg = _abi.make_config(solver="EulerRoe", size=(n, n), boundary="PERIODIC", limiter="MinMod",
+                               integrator="RungeKutta2")
+        u0 = ic.kelvin_helmholtz(size=(n, n), seed=100 + k).reshape(-1)
+        s_ = hg.Solver(cfg)
+        s_.resetState(u0)
+        if k == 0:
+            s_.update(3, want_dt=False)
+            s_.resetState(u0)
+        plain_ms += s_.timed_update(args.adjoint_steps)
+        s_.resetState(u0)
+        cp = hg.Checkpoints(s_, args.adjoint_steps, 20)
+        cp.forward()
+        dts = cp.dts()
+        uT = s_.getState().copy()
+        target = uT.reshape(shape)[..., 0] + pert
+        loss, lamT = loss_and_cotangent(uT, target)
+        dl = torch.tensor(lamT, device="cuda")
+        g = torch.empty_like(dl)
+        torch.cuda.synchronize()
+        cp.backward(dl.data_ptr(), g.data_ptr())
+        s_.synchronize()
+        f, bw = cp.times()
+        fwd_ms += f
+        bwd_ms += bw
+        if k == 0 and args.fd_directions > 0:
+            gh = g.cpu().numpy()
+            rng = np.random.default_rng(300)
+            errs = []
+            for _ in range(args.fd_directions):
+                d = rng.standard_normal(u0.size)
+                d /= np.linalg.norm(d)
+                vals = []
+                for sgn in (1, -1):
+                    s_.resetState(u0 + sgn * 1e-6 * d)
+                    s_.update_frozen_dt(dts)
+                    vals.append(loss_and_cotangent(s_.getState(), target)[0])
+                fdv = (vals[0] - vals[1]) / 2e-6
+                ad = float(np.dot(gh, d))
+                errs.append(abs(fdv - ad) / abs(ad))
+            errs = np.array(errs)
+            fd = {"directions": len(errs), "eps": 1e-6, "rel_err_median": float(np.median(errs)),
+                  "rel_err_max": float(errs.max()), "within_1e-6": int((errs <= 1e-6).sum()),
+                  "note": "MinMod and the upwind choice have kinks; on this noisy state perturbations cross "
+                          "some of them, so a difference quotient is not a derivative everywhere"}
+        cp.close()
+        s_.close()
+    fd_smooth = smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, pert) if args.fd_directions > 0 else None
+    steps_total = args.adjoint_steps * args.adjoint_problems
+    return {
+        "workload": "%d x KH 512^2 (seeds 100..), EulerRoe RK2 MinMod FP64, %d steps, checkpoints every 20"
+                    % (args.adjoint_problems, args.adjoint_steps),
+        "forward_ms_per_step": fwd_ms / steps_total, "plain_forward_ms_per_step": plain_ms / steps_total,
+        "backward_ms_per_step": bwd_ms / steps_total,
+        "adjoint_over_forward": bwd_ms / fwd_ms, "adjoint_over_plain_forward": bwd_ms / plain_ms,
+        "finite_differences": fd,
+        "finite_differences_differentiable": fd_smooth,
+    }
+
+
 def run_gb300(args):
     rank, local_rank, world = dist_env()
     pg = None
@@ -312,7 +513,12 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_sample(size)
 
-    fp64_per_cell_update = None
+    batched = adjoint = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        batched = batched_sweep(hg, _abi, ic, args)
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        adjoint = adjoint_measure(hg, _abi, ic, args)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -327,6 +533,8 @@ def run_gb300(args):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
+        "batched_sweep": batched,
+        "adjoint": adjoint,
         "gpu_launches": kernels_per_step * args.steps,
         "health_flags": health,
     }
