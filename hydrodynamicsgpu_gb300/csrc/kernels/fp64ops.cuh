@@ -76,4 +76,90 @@ __device__ __forceinline__ double divByRecip(double x, double b, double rb) {
 }
 __device__ __forceinline__ float divByRecip(float x, float b, float rb) { return x / b; }
 
+// x * y computed on the integer pipes, bit-identical to the FP64 unit's product.
+// The FP64 unit issues 2 operations per SM per clock on this part while the integer
+// and FP32 pipes stand idle in the FP64-bound kernels; products routed here run on
+// those pipes, concurrently with the native adds.  Fast path: both operands normal
+// and the biased exponent sum in [1, 2045]; the 53 x 53-bit significand product is
+// formed exactly (106 bits) and rounded to nearest, ties to even; the carry of a
+// round-up into bit 53 increments the exponent field (to +-Inf only from the largest
+// binade, as IEEE 754 requires).  Zeros, subnormals, Inf, NaN and products that could
+// leave the normal range take the FP64 unit.  Checked against the FP64 unit on 4.3e9
+// random operand pairs (all exponent ranges, short significands, extremes).
+// the rare native product, kept out of line: inlined, it would be if-converted and
+// issued to the FP64 unit for every operand pair
+static __device__ __noinline__ double mulNative(double x, double y) { return x * y; }
+
+__device__ __forceinline__ double mulI(double x, double y) {
+    const unsigned long long ux = (unsigned long long)bitsOf(x), uy = (unsigned long long)bitsOf(y);
+    const unsigned ex = (unsigned)(ux >> 52) & 0x7FF, ey = (unsigned)(uy >> 52) & 0x7FF;
+    int e = (int)ex + (int)ey - 1023;
+    if (ex - 1u >= 2046u || ey - 1u >= 2046u || (unsigned)(e - 1) >= 2045u) return mulNative(x, y);
+    const unsigned long long mx = (ux & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const unsigned long long my = (uy & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const unsigned long long lo = mx * my, hi = __umul64hi(mx, my);   // product in [2^104, 2^106)
+    unsigned long long mant, rest;
+    if (hi >> 41) {
+        mant = (hi << 11) | (lo >> 53);
+        rest = lo << 11;
+        e += 1;
+    } else {
+        mant = (hi << 12) | (lo >> 52);
+        rest = lo << 12;
+    }
+    // rest: the round bit on top, the sticky bits below it
+    mant += (rest > 0x8000000000000000ull) || (rest == 0x8000000000000000ull && (mant & 1));
+    const unsigned long long r = (((unsigned long long)(e - 1) << 52) + mant) | ((ux ^ uy) & 0x8000000000000000ull);
+    return fromBits((long long)r);
+}
+__device__ __forceinline__ float mulI(float x, float y) { return x * y; }
+
+static __device__ __noinline__ double divNative(double x, double y) { return x / y; }
+
+// x / y on the integer pipes, bit-identical to the IEEE quotient (round to nearest
+// even).  Fast path: both operands normal and the quotient's biased exponent safely
+// inside [1, 2046].  With m_x, m_y the 53-bit significands and s = [m_x < m_y], the
+// truncated quotient q = floor(m_x 2^(52+s) / m_y) lies in [2^52, 2^53).  A reciprocal
+// v ~ 2^126 / (m_y 2^11) is seeded from the FP32 reciprocal of m_y's top 24 bits
+// (relative error below 2^-22) and refined by two fixed-point Newton steps
+// v += v (2^126 - m_y 2^11 v) / 2^126; q is estimated as (m_x v) >> (63 - s), the
+// remainder r = m_x 2^(52+s) - q m_y is formed exactly modulo 2^64 (|r| < 2^63) and
+// q corrected until 0 <= r < m_y; then q is rounded up when 2r > m_y, or 2r = m_y
+// and q is odd.  Everything else takes the FP64 unit.  Checked against the FP64
+// unit's quotient on 4.3e9 random operand pairs.
+__device__ __forceinline__ double divI(double x, double y) {
+    const unsigned long long ux = (unsigned long long)bitsOf(x), uy = (unsigned long long)bitsOf(y);
+    const unsigned ex = (unsigned)(ux >> 52) & 0x7FF, ey = (unsigned)(uy >> 52) & 0x7FF;
+    int e = (int)ex - (int)ey + 1023;
+    if (ex - 1u >= 2046u || ey - 1u >= 2046u || (unsigned)(e - 2) >= 2044u) return divNative(x, y);
+    const unsigned long long mx = (ux & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const unsigned long long d = (uy & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const unsigned s = mx < d;
+    e -= (int)s;
+    const unsigned long long dn = d << 11;                                   // [2^63, 2^64)
+    const float rf = __frcp_rn((float)(unsigned)(dn >> 40));                // exact operand in [2^23, 2^24)
+    unsigned long long v = __float2ull_rz(rf * 7.737125245533627e25f);       // rf * 2^86, in (2^62, 2^63]
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const unsigned long long plo = dn * v, phi = __umul64hi(dn, v);
+        const long long eh = (long long)(0x4000000000000000ull - phi) - (plo != 0);   // floor((2^126 - dn v) / 2^64)
+        const unsigned long long mag = (unsigned long long)(eh < 0 ? -eh : eh);
+        const unsigned long long corr = (__umul64hi(v, mag) << 2) | ((v * mag) >> 62);   // v |eh| / 2^62
+        v = eh < 0 ? v - corr : v + corr;
+    }
+    const unsigned long long hi = __umul64hi(mx, v), lo = mx * v;
+    unsigned long long q = s ? ((hi << 2) | (lo >> 62)) : ((hi << 1) | (lo >> 63));
+    long long r = (long long)((mx << (52 + s)) - q * d);
+    if (r < 0) { q -= 1; r += (long long)d; }
+    if (r < 0) { q -= 1; r += (long long)d; }
+    if (r >= (long long)d) { q += 1; r -= (long long)d; }
+    if (r >= (long long)d) { q += 1; r -= (long long)d; }
+    const unsigned long long r2 = (unsigned long long)r << 1;
+    q += (r2 > d) || (r2 == d && (q & 1));
+    return fromBits((long long)((((unsigned long long)(e - 1) << 52) + q) | ((ux ^ uy) & 0x8000000000000000ull)));
+}
+__device__ __forceinline__ float divI(float x, float y) { return x / y; }
+
+
+
 }  // namespace hgpu

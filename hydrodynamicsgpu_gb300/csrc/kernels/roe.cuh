@@ -55,20 +55,20 @@ __device__ __forceinline__ void roePrim(const real* s, real gamma, RoePrim<real,
     const int E = D + 1;
     const real gm1 = gamma - (real)1.f;
     real rho = s[0];
-    real invDensity = (real)1.f / rho;                                   // `1.f / density`
+    real invDensity = divI((real)1.f, rho);                              // `1.f / density`
     // VELOCITY(ptr) = (m..., 0)/rho componentwise (res/include/HydroGPU/Euler.h:6-12);
     // m/rho by the correction step on RN(1/rho) (fp64ops.cuh) is the same quotient
 #pragma unroll
     for (int k = 0; k < D; ++k) P.v[k] = divByRecip(s[1 + k], rho, invDensity);
     // dot(v,v) over 4 components; the zero components add +0 to a non-negative sum
-    real vv = P.v[0] * P.v[0];
+    real vv = mulI(P.v[0], P.v[0]);
 #pragma unroll
-    for (int k = 1; k < D; ++k) vv = vv + P.v[k] * P.v[k];
-    real energyTotal = s[E] * invDensity;
+    for (int k = 1; k < D; ++k) vv = vv + mulI(P.v[k], P.v[k]);
+    real energyTotal = mulI(s[E], invDensity);
     real energyKinetic = halfOf(vv);                                     // .5f * dot(v, v)
     real energyInternal = energyTotal - energyKinetic;                   // - potential (0)
-    real pressure = gm1 * rho * energyInternal;
-    P.h = energyTotal + pressure * invDensity;
+    real pressure = mulI(mulI(gm1, rho), energyInternal);
+    P.h = energyTotal + mulI(pressure, invDensity);
     P.w = sqrt(rho);
 }
 
@@ -79,21 +79,21 @@ __device__ __forceinline__ void roeBasisFromPrim(const RoePrim<real, D>& L, cons
     typedef RoeRec<D> R_;
     const int E = D + 1;
     const real gm1 = gamma - (real)1.f;
-    real norm = (real)1.f / (L.w + R.w);
+    real norm = divI((real)1.f, L.w + R.w);
     real v[3];
 #pragma unroll
-    for (int k = 0; k < D; ++k) v[k] = (L.w * L.v[k] + R.w * R.v[k]) * norm;
-    real enthalpyTotal = (L.w * L.h + R.w * R.h) * norm;
-    real velocitySq = v[0] * v[0];
+    for (int k = 0; k < D; ++k) v[k] = mulI(mulI(L.w, L.v[k]) + mulI(R.w, R.v[k]), norm);
+    real enthalpyTotal = mulI(mulI(L.w, L.h) + mulI(R.w, R.h), norm);
+    real velocitySq = mulI(v[0], v[0]);
 #pragma unroll
-    for (int k = 1; k < D; ++k) velocitySq = velocitySq + v[k] * v[k];
-    real c = sqrt((enthalpyTotal - halfOf(velocitySq)) * gm1);          // - energyPotential (0)
+    for (int k = 1; k < D; ++k) velocitySq = velocitySq + mulI(v[k], v[k]);
+    real c = sqrt(mulI(enthalpyTotal - halfOf(velocitySq), gm1));       // - energyPotential (0)
     // rotate: normal velocity first (res/EulerRoe.cl:101-110)
     real vx = v[SIDE];
     real vt[2] = {0, 0};
     if (D > 1) vt[0] = (SIDE == 1) ? v[0] : v[1];
     if (D > 2) vt[1] = (SIDE == 2) ? v[0] : v[2];
-    real cvx = c * vx;
+    real cvx = mulI(c, vx);
     rec[R_::LAM0] = vx - c;
     rec[R_::VX] = vx;
     rec[R_::LAME] = vx + c;
@@ -102,21 +102,21 @@ __device__ __forceinline__ void roeBasisFromPrim(const RoePrim<real, D>& L, cons
 #pragma unroll
     for (int t = 0; t < D - 1; ++t) rec[R_::VT + t] = vt[t];
     rec[R_::HP] = enthalpyTotal + cvx;
-    real invDenom = (real).5f / (c * c);
-    real hv = (real).5f * gm1 * velocitySq;                              // .5f * (gamma - 1.f) * velocitySq
-    real gvx = gm1 * vx;
-    rec[R_::L0 + 0] = (hv + cvx) * invDenom;
-    rec[R_::L0 + 1] = -(c + gvx) * invDenom;
+    real invDenom = divI((real).5f, mulI(c, c));
+    real hv = mulI(mulI((real).5f, gm1), velocitySq);                    // .5f * (gamma - 1.f) * velocitySq
+    real gvx = mulI(gm1, vx);
+    rec[R_::L0 + 0] = mulI(hv + cvx, invDenom);
+    rec[R_::L0 + 1] = mulI(-(c + gvx), invDenom);
 #pragma unroll
-    for (int t = 0; t < D - 1; ++t) rec[R_::L0 + 2 + t] = -gm1 * vt[t] * invDenom;
-    rec[R_::L0 + E] = gm1 * invDenom;
-    rec[R_::L1 + 0] = (real)1.f - gm1 * velocitySq * invDenom;
-    rec[R_::L1 + 1] = gvx * (real)2.f * invDenom;
+    for (int t = 0; t < D - 1; ++t) rec[R_::L0 + 2 + t] = mulI(mulI(-gm1, vt[t]), invDenom);
+    rec[R_::L0 + E] = mulI(gm1, invDenom);
+    rec[R_::L1 + 0] = (real)1.f - mulI(mulI(gm1, velocitySq), invDenom);
+    rec[R_::L1 + 1] = mulI(mulI(gvx, (real)2.f), invDenom);
 #pragma unroll
-    for (int t = 0; t < D - 1; ++t) rec[R_::L1 + 2 + t] = gm1 * vt[t] * (real)2.f * invDenom;
-    rec[R_::L1 + E] = -gm1 * (real)2.f * invDenom;
-    rec[R_::LE0] = (hv - cvx) * invDenom;
-    rec[R_::LE1] = (c - gvx) * invDenom;
+    for (int t = 0; t < D - 1; ++t) rec[R_::L1 + 2 + t] = mulI(mulI(mulI(gm1, vt[t]), (real)2.f), invDenom);
+    rec[R_::L1 + E] = mulI(mulI(-gm1, (real)2.f), invDenom);
+    rec[R_::LE0] = mulI(hv - cvx, invDenom);
+    rec[R_::LE1] = mulI(c - gvx, invDenom);
 }
 
 // Eigen basis of one interface from the two cell states.
@@ -187,19 +187,19 @@ __device__ __forceinline__ void leftTransform(const real* rec, const real* x, re
     if (!allFinite<real, N>(x)) { leftTransformDense<real, D, SIDE>(rec, x, y); return; }
     // row 0 and row 1: dense
     {
-        real s0 = zfix(rec[R_::L0 + perm<SIDE>(0)] * x[0]);
-        real s1 = zfix(rec[R_::L1 + perm<SIDE>(0)] * x[0]);
+        real s0 = zfix(mulI(rec[R_::L0 + perm<SIDE>(0)], x[0]));
+        real s1 = zfix(mulI(rec[R_::L1 + perm<SIDE>(0)], x[0]));
 #pragma unroll
         for (int j = 1; j < N; ++j) {
-            s0 = s0 + rec[R_::L0 + perm<SIDE>(j)] * x[j];
-            s1 = s1 + rec[R_::L1 + perm<SIDE>(j)] * x[j];
+            s0 = s0 + mulI(rec[R_::L0 + perm<SIDE>(j)], x[j]);
+            s1 = s1 + mulI(rec[R_::L1 + perm<SIDE>(j)], x[j]);
         }
         y[0] = s0;
         y[1] = s1;
     }
     // tangent rows t = 2..E-1: [-vt, 0, .., 1 (column t), .., 0] in the normal frame
 #pragma unroll
-    for (int t = 2; t < E; ++t) y[t] = zfix(-rec[R_::VT + t - 2] * x[0]) + x[perm<SIDE>(t)];
+    for (int t = 2; t < E; ++t) y[t] = zfix(mulI(-rec[R_::VT + t - 2], x[0])) + x[perm<SIDE>(t)];
     // row E: [LE0, LE1, L0[2..]] in the normal frame
     {
         real s = 0;
@@ -207,7 +207,7 @@ __device__ __forceinline__ void leftTransform(const real* rec, const real* x, re
         for (int j = 0; j < N; ++j) {
             int c = perm<SIDE>(j);
             real m = c == 0 ? rec[R_::LE0] : (c == 1 ? rec[R_::LE1] : rec[R_::L0 + c]);
-            s = (j == 0) ? zfix(m * x[0]) : s + m * x[j];
+            s = (j == 0) ? zfix(mulI(m, x[0])) : s + mulI(m, x[j]);
         }
         y[E] = s;
     }
@@ -223,19 +223,19 @@ __device__ __forceinline__ void rightTransform(const real* rec, const real* f, r
     // row 0: [1, 1, 0.., 1]
     Fr[0] = zfix(f[0]) + f[1] + f[E];
     // row 1: [lam0, vx, 0.., lamE]
-    Fr[1] = zfix(rec[R_::LAM0] * f[0]) + rec[R_::VX] * f[1] + rec[R_::LAME] * f[E];
+    Fr[1] = zfix(mulI(rec[R_::LAM0], f[0])) + mulI(rec[R_::VX], f[1]) + mulI(rec[R_::LAME], f[E]);
     // tangent rows t: [vt, vt, (1 at column t), vt]
 #pragma unroll
     for (int t = 2; t < E; ++t) {
         real vt = rec[R_::VT + t - 2];
-        Fr[t] = ((zfix(vt * f[0]) + vt * f[1]) + f[t]) + vt * f[E];
+        Fr[t] = ((zfix(mulI(vt, f[0])) + mulI(vt, f[1])) + f[t]) + mulI(vt, f[E]);
     }
     // row E: [H - c vx, .5 v^2, vt..., H + c vx]
     {
-        real s = zfix(rec[R_::HM] * f[0]) + rec[R_::HV2] * f[1];
+        real s = zfix(mulI(rec[R_::HM], f[0])) + mulI(rec[R_::HV2], f[1]);
 #pragma unroll
-        for (int t = 2; t < E; ++t) s = s + rec[R_::VT + t - 2] * f[t];
-        Fr[E] = s + rec[R_::HP] * f[E];
+        for (int t = 2; t < E; ++t) s = s + mulI(rec[R_::VT + t - 2], f[t]);
+        Fr[E] = s + mulI(rec[R_::HP], f[E]);
     }
 #pragma unroll
     for (int g = 0; g < N; ++g) F[g] = Fr[perm<SIDE>(g)];
@@ -262,21 +262,21 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
     const real vx = rec[R_::VX];
     const bool midUp = geZero(vx);
     const real midTheta = midUp ? (real)1. : (real)-1.;
-    const real midEps = vx * dt_dx;
+    const real midEps = mulI(vx, dt_dx);
     const real midEpsTheta = midEps - midTheta;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         const bool mid = i > 0 && i < N - 1;
         real eigenvalue = roeEigenvalue<real, D>(rec, i);
-        ft[i] = ft[i] * eigenvalue;
+        ft[i] = mulI(ft[i], eigenvalue);
         bool up = mid ? midUp : geZero(eigenvalue);
-        real rTilde = (up ? dqL[i] : dqR[i]) / dq[i];
+        real rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
         real theta = mid ? midTheta : (up ? (real)1. : (real)-1.);
         real phi = slopeLimiter<real>(lim, rTilde);
-        real epsMinusTheta = mid ? midEpsTheta : eigenvalue * dt_dx - theta;
-        real deltaFluxTilde = eigenvalue * dq[i];
+        real epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
+        real deltaFluxTilde = mulI(eigenvalue, dq[i]);
         // `fluxTilde[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta))`
-        if (sizeof(real) == 8) ft[i] = ft[i] - halfOf(deltaFluxTilde) * (theta + phi * epsMinusTheta);
+        if (sizeof(real) == 8) ft[i] = ft[i] - mulI(halfOf(deltaFluxTilde), theta + mulI(phi, epsMinusTheta));
         else ft[i] -= .5 * deltaFluxTilde * (theta + phi * epsMinusTheta);   // double literal: FP32 promotes
     }
     rightTransform<real, D, SIDE>(rec, ft, F);

@@ -89,7 +89,7 @@ __device__ __forceinline__ unsigned long long roeDtCell(const Grid& g, const Phy
         real lamMin = basis[((long long)side * R_::NB + R_::LAM0) * g.V + c + g.step[side]];
         real maxLambda = fmaxLibm((real)0., lamMax);
         real minLambda = fminLibm((real)0., lamMin);
-        real dum = (real)((double)ph.dx[side] / ((double)fabs(maxLambda - minLambda) + 1e-9));
+        real dum = (real)divI((double)ph.dx[side], (double)fabs(maxLambda - minLambda) + 1e-9);
         if (dum != dum) nan = true;
         unsigned long long b = realBits(dum);
         best = b < best ? b : best;
