@@ -54,6 +54,8 @@ SIGNATURES = {
     "hgpu_checkpoint_backward": (ctypes.c_int, [_P, _P, _P]),
     "hgpu_checkpoint_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "hgpu_checkpoint_destroy": (ctypes.c_int, [_P]),
+    "hgpu_fp64_selftest": (ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong),
+                                          ctypes.POINTER(ctypes.c_longlong)]),
     "hgpu_batch_create": (ctypes.c_int, [_CFG, ctypes.c_int, ctypes.POINTER(_P)]),
     "hgpu_batch_destroy": (ctypes.c_int, [_P]),
     "hgpu_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
@@ -76,6 +78,13 @@ class KernelTime(ctypes.Structure):
 
 def select_device(device):
     check(lib().hgpu_select_device(int(device)))
+
+
+def fp64_selftest(cases=1 << 26, seed=1):
+    """(mul, div) mismatches of the integer-pipe binary64 product/quotient against the FP64 unit."""
+    m, d = ctypes.c_longlong(), ctypes.c_longlong()
+    check(lib().hgpu_fp64_selftest(int(seed), int(cases), ctypes.byref(m), ctypes.byref(d)))
+    return m.value, d.value
 
 
 def fp64_peak():

@@ -23,7 +23,7 @@ SOURCES = {
     "kernels/roe.cu": ["--fmad=false"],
     "kernels/hllc.cu": ["--fmad=false"],
     "kernels/combine.cu": ["--fmad=false"],
-    "kernels/probe.cu": [],
+    "kernels/probe.cu": ["--fmad=false"],
     "kernels/noalloc.cu": ["--fmad=false"],
     "kernels/batch.cu": ["--fmad=false"],
     "kernels/adjoint.cu": [],

@@ -12,6 +12,7 @@
 
 namespace hgpu {
 double measureFp64FmaRate();
+int selftestFp64Ops(unsigned long long seed, long long cases, long long* mulBad, long long* divBad);
 void setLastError(const std::string& msg);
 }
 
@@ -488,6 +489,16 @@ int hgpu_batch_autotune(hgpu_batch* b, const char* cache_path, int steps) {
     if (!b || steps <= 0) return fail(HGPU_ERR_ARG, "bad argument");
     return guarded([&]() {
         b->b->autotune(cache_path ? std::string(cache_path) : std::string(), steps);
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_fp64_selftest(unsigned long long seed, long long cases, long long* mul_mismatches,
+                       long long* div_mismatches) {
+    if (!mul_mismatches || !div_mismatches || cases < 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        if (hgpu::selftestFp64Ops(seed, cases, mul_mismatches, div_mismatches) != 0)
+            throw hgpu::CudaError(cudaGetLastError(), "fp64 self-test");
         return (int)HGPU_OK;
     });
 }

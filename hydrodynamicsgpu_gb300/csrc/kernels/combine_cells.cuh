@@ -117,7 +117,7 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
         real dt = sc.dt;
         real* s = plan.slot[0] + (long long)N * (off + c);
 #pragma unroll
-        for (int j = 0; j < N; ++j) s[j] = s[j] + d[j] * dt;
+        for (int j = 0; j < N; ++j) s[j] = s[j] + mulI(d[j], dt);
         return;
     }
     real u[N];
@@ -136,7 +136,7 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
         if (op.hasAlpha) {
 #pragma unroll
             for (int j = 0; j < N; ++j) {
-                real t = op.alphaIsOne ? u[j] : u[j] * op.alpha;
+                real t = op.alphaIsOne ? u[j] : mulI(u[j], op.alpha);
                 v[j] = empty ? zfix(t) : v[j] + t;
             }
             empty = false;
@@ -145,7 +145,7 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
             real cf = sc.coef[op.brow][op.bcol];
 #pragma unroll
             for (int j = 0; j < N; ++j) {
-                real t = d[j] * cf;
+                real t = mulI(d[j], cf);
                 v[j] = empty ? zfix(t) : v[j] + t;
             }
         }

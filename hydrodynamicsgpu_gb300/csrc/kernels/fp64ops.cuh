@@ -56,25 +56,7 @@ __device__ __forceinline__ double fmaxLibm(double x, double y) {
 __device__ __forceinline__ float fminLibm(float x, float y) { return (x < y || y != y) ? x : y; }
 __device__ __forceinline__ float fmaxLibm(float x, float y) { return (x > y || y != y) ? x : y; }
 
-// x / b given rb = RN(1/b) (b and rb normal): Markstein's quotient correction,
-//   q = RN(x*rb), r = x - b*q (exact, by fma), q' = RN(q + r*rb) = RN(x/b)
-// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
-// processor", IBM J. Res. Dev. 34(1), 1990; checked here against the hardware
-// division on 3.8e9 random and near-midpoint operand pairs, none differing).
-// A zero x over a finite nonzero b gives the zero of sign(x) xor sign(b); operands
-// outside a safe exponent window (zero, subnormal, huge, Inf, NaN -- so 0/0 and x/0
-// too) take the hardware division, so q' and r never leave the normal range.
-__device__ __forceinline__ double divByRecip(double x, double b, double rb) {
-    long long bx = bitsOf(x), bb = bitsOf(b);
-    int ex = (int)((bx >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
-    if ((bx & 0x7FFFFFFFFFFFFFFFLL) == 0 && eb != 0 && eb != 0x7FF)
-        return fromBits((bx ^ bb) & (long long)0x8000000000000000ULL);
-    if (ex < 623 || ex > 1423 || eb < 623 || eb > 1423) return x / b;
-    double q = x * rb;
-    double r = fma(-b, q, x);
-    return fma(r, rb, q);
-}
-__device__ __forceinline__ float divByRecip(float x, float b, float rb) { return x / b; }
+
 
 // x * y computed on the integer pipes, bit-identical to the FP64 unit's product.
 // The FP64 unit issues 2 operations per SM per clock on this part while the integer
@@ -113,6 +95,26 @@ __device__ __forceinline__ double mulI(double x, double y) {
     return fromBits((long long)r);
 }
 __device__ __forceinline__ float mulI(float x, float y) { return x * y; }
+
+// x / b given rb = RN(1/b) (b and rb normal): Markstein's quotient correction,
+//   q = RN(x*rb), r = x - b*q (exact, by fma), q' = RN(q + r*rb) = RN(x/b)
+// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990; checked here against the hardware
+// division on 3.8e9 random and near-midpoint operand pairs, none differing).
+// A zero x over a finite nonzero b gives the zero of sign(x) xor sign(b); operands
+// outside a safe exponent window (zero, subnormal, huge, Inf, NaN -- so 0/0 and x/0
+// too) take the hardware division, so q' and r never leave the normal range.
+__device__ __forceinline__ double divByRecip(double x, double b, double rb) {
+    long long bx = bitsOf(x), bb = bitsOf(b);
+    int ex = (int)((bx >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
+    if ((bx & 0x7FFFFFFFFFFFFFFFLL) == 0 && eb != 0 && eb != 0x7FF)
+        return fromBits((bx ^ bb) & (long long)0x8000000000000000ULL);
+    if (ex < 623 || ex > 1423 || eb < 623 || eb > 1423) return x / b;
+    double q = mulI(x, rb);
+    double r = fma(-b, q, x);
+    return fma(r, rb, q);
+}
+__device__ __forceinline__ float divByRecip(float x, float b, float rb) { return x / b; }
 
 static __device__ __noinline__ double divNative(double x, double y) { return x / y; }
 

@@ -1,7 +1,10 @@
-// probe.cu -- FP64 fused multiply-add issue-rate probe (the FP64 roofline denominator).
-// Eight independent dependency chains per thread keep the FP64 pipe busy; every
-// thread writes one result, so nothing is optimised away and every store is in bounds.
+// probe.cu -- FP64 fused multiply-add issue-rate probe (the FP64 roofline denominator),
+// and a self-test of the integer-pipe product and quotient (fp64ops.cuh) against the
+// FP64 unit.  Eight independent dependency chains per thread keep the FP64 pipe busy;
+// every thread writes one result, so nothing is optimised away and every store is in bounds.
 #include <cuda_runtime.h>
+
+#include "fp64ops.cuh"
 
 namespace hgpu {
 namespace {
@@ -14,7 +17,59 @@ __global__ void __launch_bounds__(256) dfmaProbe(double* out, double a, double b
     }
     out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
 }
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// operand classes: any exponent (zeros, subnormals, Inf/NaN included), moderate
+// exponents, short significands (exact products/quotients, powers of two), extremes
+__device__ double operand(unsigned long long s, int cls) {
+    const unsigned long long r = splitmix(s), m = r & 0xFFFFFFFFFFFFFull, sg = (r >> 63) << 63;
+    const unsigned long long t = splitmix(s ^ 0x5bd1e995ull);
+    unsigned e;
+    unsigned long long mm = m;
+    if (cls == 0) e = (unsigned)(t % 2048);
+    else if (cls == 1) e = 1023 - 60 + (unsigned)(t % 120);
+    else if (cls == 2) { e = 1023 - 4 + (unsigned)(t % 8); mm = m & ~((1ull << (t >> 32) % 53) - 1); }
+    else e = (t & 1) ? (unsigned)(t % 40) : 2047 - (unsigned)(t % 40);
+    return fromBits((long long)(sg | ((unsigned long long)e << 52) | mm));
+}
+
+__global__ void selftestKernel(unsigned long long seed, long long cases, unsigned long long* bad) {
+    unsigned long long nm = 0, nd = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cases;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long s = splitmix(seed + (unsigned long long)i);
+        const double x = operand(s, (int)(s % 4)), y = operand(s ^ 0xabcdefull, (int)((s >> 8) % 4));
+        const double pm = x * y, qm = mulI(x, y), pd = x / y, qd = divI(x, y);
+        if (bitsOf(pm) != bitsOf(qm) && !(pm != pm && qm != qm)) ++nm;
+        if (bitsOf(pd) != bitsOf(qd) && !(pd != pd && qd != qd)) ++nd;
+    }
+    if (nm) atomicAdd(&bad[0], nm);
+    if (nd) atomicAdd(&bad[1], nd);
+}
 }  // namespace
+
+// mismatches of mulI / divI against the FP64 unit over `cases` seeded operand pairs
+int selftestFp64Ops(unsigned long long seed, long long cases, long long* mulBad, long long* divBad) {
+    unsigned long long* bad = nullptr;
+    if (cudaMalloc(&bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return -1;
+    cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    selftestKernel<<<sms * 8, 256>>>(seed, cases, bad);
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(h, bad, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    if (e != cudaSuccess) return -1;
+    *mulBad = (long long)h[0];
+    *divBad = (long long)h[1];
+    return 0;
+}
 
 // returns fma instructions per second over the whole device, or a negative value on error
 double measureFp64FmaRate() {

@@ -308,6 +308,12 @@ int hgpu_cfl_timestep_noalloc(const hgpu_config* cfg, const void* d_state, doubl
 /* Diagnostic: measured FP64 fused multiply-add issue rate of the current device
  * (fma instructions per second, all SMs), the denominator of the FP64 roofline. */
 int hgpu_fp64_peak(double* fma_per_second);
+/* Self-test of the kernels' integer-pipe binary64 product and quotient: compares
+ * them bit for bit with the FP64 unit on `cases` seeded operand pairs (all exponent
+ * ranges, short significands, zeros, subnormals, Inf, NaN) and returns the counts
+ * of differing results (NaN == NaN). */
+int hgpu_fp64_selftest(unsigned long long seed, long long cases, long long* mul_mismatches,
+                       long long* div_mismatches);
 
 #ifdef __cplusplus
 }
