@@ -8,6 +8,7 @@
 // entry) instead of two dense N x N matrices, and it is computed once per step
 // from u^n exactly as the reference does (Roe.cpp:82-92).  The bodies live in
 // roe_cells.cuh (shared with the batched kernels).
+#include "../../../include/hgpu/hgpu.h"
 #include "kernels.h"
 #include "reduce.cuh"
 #include "roe_cells.cuh"
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(kThreads) roeDeltaQKernel(Grid g, const real* 
     roeDeltaQCell<real, D>(g, stage, basis, dq, c, x, y, z, loA, hiA);
 }
 
-template <typename real, int D>
+template <typename real, int D, int LIM>
 __global__ void __launch_bounds__(kThreads) roeFluxKernel(Grid g, int lim, const real* __restrict__ stage,
                                                           const real* __restrict__ basis, const real* __restrict__ dq,
                                                           const StepConst<real>* __restrict__ sc,
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(kThreads) roeFluxKernel(Grid g, int lim, const
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    roeFluxCell<real, D>(g, lim, *sc, stage, basis, dq, flux, c, x, y, z);
+    roeFluxCell<real, D, LIM>(g, lim, *sc, stage, basis, dq, flux, c, x, y, z);
 }
 
 }  // namespace
@@ -114,13 +115,29 @@ void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* 
     else roeDeltaQKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
 }
 
+template <typename real, int LIM>
+void launchRoeFluxLim(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
+                      const StepConst<real>* sc, real* flux, cudaStream_t st) {
+    if (g.dim == 1) roeFluxKernel<real, 1, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+    else if (g.dim == 2) roeFluxKernel<real, 2, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+    else roeFluxKernel<real, 3, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+}
+
+// the benchmark limiters and the common ones get kernels of their own; the others
+// share one kernel that dispatches on the limiter at run time
 template <typename real>
 void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
                    const StepConst<real>* sc, real* flux, int seam, cudaStream_t st) {
     (void)seam;
-    if (g.dim == 1) roeFluxKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
-    else if (g.dim == 2) roeFluxKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
-    else roeFluxKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+    switch (limiter) {
+    case HGPU_LIMITER_DONORCELL: launchRoeFluxLim<real, HGPU_LIMITER_DONORCELL>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    case HGPU_LIMITER_LAXWENDROFF: launchRoeFluxLim<real, HGPU_LIMITER_LAXWENDROFF>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    case HGPU_LIMITER_MINMOD: launchRoeFluxLim<real, HGPU_LIMITER_MINMOD>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    case HGPU_LIMITER_VANLEER: launchRoeFluxLim<real, HGPU_LIMITER_VANLEER>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    case HGPU_LIMITER_MONOTIZEDCENTRAL: launchRoeFluxLim<real, HGPU_LIMITER_MONOTIZEDCENTRAL>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    case HGPU_LIMITER_SUPERBEE: launchRoeFluxLim<real, HGPU_LIMITER_SUPERBEE>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    default: launchRoeFluxLim<real, -1>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    }
 }
 
 #define INST(real)                                                                                              \

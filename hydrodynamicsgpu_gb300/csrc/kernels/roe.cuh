@@ -249,7 +249,9 @@ __device__ __forceinline__ real roeEigenvalue(const real* rec, int i) {
 
 // Limited characteristic flux of one interface (res/Roe.cl:253-298).
 // sL, sR: stage states; dqL, dq, dqR: Delta-q-tilde at the faces before/at/after.
-template <typename real, int D, int SIDE>
+// LIM >= 0 fixes the slope limiter at compile time (the kernel then carries one
+// limiter instead of all twenty at each of its wave sites); -1 dispatches on `lim`.
+template <typename real, int D, int SIDE, int LIM = -1>
 __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const real* sR, const real* dqL,
                                         const real* dq, const real* dqR, real dt_dx, int lim, real* F) {
     typedef RoeRec<D> R_;
@@ -272,7 +274,7 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
         bool up = mid ? midUp : geZero(eigenvalue);
         real rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
         real theta = mid ? midTheta : (up ? (real)1. : (real)-1.);
-        real phi = slopeLimiter<real>(lim, rTilde);
+        real phi = slopeLimiter<real>(LIM >= 0 ? LIM : lim, rTilde);
         real epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
         real deltaFluxTilde = mulI(eigenvalue, dq[i]);
         // `fluxTilde[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta))`
