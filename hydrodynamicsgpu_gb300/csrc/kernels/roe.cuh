@@ -264,21 +264,23 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
     const real vx = rec[R_::VX];
     const bool midUp = geZero(vx);
     const real midTheta = midUp ? (real)1. : (real)-1.;
-    const real midEps = mulI(vx, dt_dx);
+    const real midEps = vx * dt_dx;
     const real midEpsTheta = midEps - midTheta;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         const bool mid = i > 0 && i < N - 1;
         real eigenvalue = roeEigenvalue<real, D>(rec, i);
-        ft[i] = mulI(ft[i], eigenvalue);
+        ft[i] = ft[i] * eigenvalue;
         bool up = mid ? midUp : geZero(eigenvalue);
         real rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
         real theta = mid ? midTheta : (up ? (real)1. : (real)-1.);
         real phi = slopeLimiter<real>(LIM >= 0 ? LIM : lim, rTilde);
-        real epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
-        real deltaFluxTilde = mulI(eigenvalue, dq[i]);
+        real epsMinusTheta = mid ? midEpsTheta : eigenvalue * dt_dx - theta;
+        real deltaFluxTilde = eigenvalue * dq[i];
         // `fluxTilde[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta))`
-        if (sizeof(real) == 8) ft[i] = ft[i] - mulI(halfOf(deltaFluxTilde), theta + mulI(phi, epsMinusTheta));
+        // (the per-wave products stay on the FP64 unit: they lie on the critical path
+        // between the two transforms, whose products run on the integer pipes)
+        if (sizeof(real) == 8) ft[i] = ft[i] - halfOf(deltaFluxTilde) * (theta + phi * epsMinusTheta);
         else ft[i] -= .5 * deltaFluxTilde * (theta + phi * epsMinusTheta);   // double literal: FP32 promotes
     }
     rightTransform<real, D, SIDE>(rec, ft, F);
