@@ -24,18 +24,18 @@ template <typename real, int D>
 __device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real, D>& p) {
     const int E = D + 1;
     p.density = st[0];
-    p.invDensity = (real)(1. / (double)p.density);
+    p.invDensity = (real)divI(1., (double)p.density);
     // VELOCITY: m/rho, by the correction step on RN(1/rho) in FP64 (fp64ops.cuh)
 #pragma unroll
     for (int k = 0; k < D; ++k) p.v[k] = divByRecip(st[1 + k], p.density, p.invDensity);
-    p.velocitySq = p.v[0] * p.v[0];
+    p.velocitySq = mulI(p.v[0], p.v[0]);
 #pragma unroll
-    for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + p.v[k] * p.v[k];
-    p.energyTotal = st[E] * p.invDensity;
+    for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + mulI(p.v[k], p.v[k]);
+    p.energyTotal = mulI(st[E], p.invDensity);
     real energyKinetic = halfOf(p.velocitySq);                          // .5f * velocitySq
     real energyInternal = p.energyTotal - energyKinetic;
-    p.pressure = (real)(((double)gamma - 1.) * (double)p.density * (double)energyInternal);
-    p.enthalpyTotal = p.energyTotal + p.pressure * p.invDensity;
+    p.pressure = (real)mulI(mulI((double)gamma - 1., (double)p.density), (double)energyInternal);
+    p.enthalpyTotal = p.energyTotal + mulI(p.pressure, p.invDensity);
 }
 
 // sl, sr of one face (EulerHLLC.cl:85-97)
@@ -49,16 +49,19 @@ __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, do
     Prim<real, D> L, R;
     primitives<real, D>(sL, ph.gamma, L);
     primitives<real, D>(sR, ph.gamma, R);
-    real cL = (real)sqrt(gm1 * (double)(L.enthalpyTotal - halfOf(L.velocitySq)));
-    real cR = (real)sqrt(gm1 * (double)(R.enthalpyTotal - halfOf(R.velocitySq)));
+    real cL = (real)sqrt(mulI(gm1, (double)(L.enthalpyTotal - halfOf(L.velocitySq))));
+    real cR = (real)sqrt(mulI(gm1, (double)(R.enthalpyTotal - halfOf(R.velocitySq))));
     // .5f * (pL + pR) - .5f * (vR - vL) * .5f * (rhoL + rhoR) * .5f * (cL + cR), halvings exact
     real pressureStar = (real)fmaxLibm(0., (double)(halfOf(L.pressure + R.pressure) -
-                                                    halfOf(halfOf(halfOf(R.v[0] - L.v[0])) * (L.density + R.density)) *
-                                                        (cL + cR)));
-    real qL = pressureStar <= L.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / L.pressure) - 1.));
-    real qR = pressureStar <= R.pressure ? (real)1. : (real)sqrt(1. + gq * ((double)(pressureStar / R.pressure) - 1.));
-    waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - cL * qL;
-    waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + cR * qR;
+                                                    mulI(halfOf(mulI(halfOf(halfOf(R.v[0] - L.v[0])),
+                                                                     L.density + R.density)),
+                                                         cL + cR)));
+    real qL = pressureStar <= L.pressure ? (real)1.
+                                         : (real)sqrt(1. + mulI(gq, (double)divI(pressureStar, L.pressure) - 1.));
+    real qR = pressureStar <= R.pressure ? (real)1.
+                                         : (real)sqrt(1. + mulI(gq, (double)divI(pressureStar, R.pressure) - 1.));
+    waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - mulI(cL, qL);
+    waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + mulI(cR, qR);
 }
 
 // wave speeds of the faces of one cell: every axis in [2, S-2] (EulerHLLC.cl:110-131)
@@ -86,7 +89,7 @@ __device__ __forceinline__ unsigned long long hllcDtCell(const Grid& g, const Ph
             real slNext = waves[((long long)side * 2 + 0) * g.V + c + g.step[side]];
             real minLambda = (real)fminLibm(0., (double)slNext);
             real maxLambda = (real)fmaxLibm(0., (double)srHere);
-            real dum = ph.dx[side] / (maxLambda - minLambda);
+            real dum = divI(ph.dx[side], maxLambda - minLambda);
             if (dum != dum) nan = true;
             result = fminLibm(result, dum);
         }
@@ -108,41 +111,42 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
     real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
     real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
     real fL[N], fR[N], flux[N];
-    fL[0] = L.density * L.v[0];
-    fL[1] = L.density * L.v[0] * L.v[0] + L.pressure;
+    fL[0] = mulI(L.density, L.v[0]);
+    fL[1] = mulI(mulI(L.density, L.v[0]), L.v[0]) + L.pressure;
 #pragma unroll
-    for (int k = 1; k < D; ++k) fL[1 + k] = L.density * L.v[k] * L.v[0];
-    fL[E] = L.density * L.enthalpyTotal * L.v[0];
-    fR[0] = R.density * R.v[0];
-    fR[1] = R.density * R.v[0] * R.v[0] + R.pressure;
+    for (int k = 1; k < D; ++k) fL[1 + k] = mulI(mulI(L.density, L.v[k]), L.v[0]);
+    fL[E] = mulI(mulI(L.density, L.enthalpyTotal), L.v[0]);
+    fR[0] = mulI(R.density, R.v[0]);
+    fR[1] = mulI(mulI(R.density, R.v[0]), R.v[0]) + R.pressure;
 #pragma unroll
-    for (int k = 1; k < D; ++k) fR[1 + k] = R.density * R.v[k] * R.v[0];
-    fR[E] = R.density * R.enthalpyTotal * R.v[0];
-    real sStar = (R.density * R.v[0] * (sr - R.v[0]) - L.density * L.v[0] * (sl - L.v[0]) + L.pressure - R.pressure) /
-                 (R.density * (sr - R.v[0]) - L.density * (sl - L.v[0]));
+    for (int k = 1; k < D; ++k) fR[1 + k] = mulI(mulI(R.density, R.v[k]), R.v[0]);
+    fR[E] = mulI(mulI(R.density, R.enthalpyTotal), R.v[0]);
+    real sStar = divI(mulI(mulI(R.density, R.v[0]), sr - R.v[0]) - mulI(mulI(L.density, L.v[0]), sl - L.v[0]) +
+                          L.pressure - R.pressure,
+                      mulI(R.density, sr - R.v[0]) - mulI(L.density, sl - L.v[0]));
     bool taken = true;
     if ((real)0. <= sl) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fL[i];
     } else if (sl <= (real)0. && (real)0. <= sStar) {
-        real pressureLR = halfOf(L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
-                                 R.density * (sr - R.v[0]) * (sStar - R.v[0]));
+        real pressureLR = halfOf(L.pressure + R.pressure + mulI(mulI(L.density, sl - L.v[0]), sStar - L.v[0]) +
+                                 mulI(mulI(R.density, sr - R.v[0]), sStar - R.v[0]));
         // every component divides by (sl - sStar): one reciprocal, then exact corrected quotients
-        real den = sl - sStar, rden = (real)1. / den;
-        flux[0] = divByRecip(sStar * (sl * stL[0] - fL[0]), den, rden);
-        flux[1] = divByRecip(sStar * (sl * stL[1] - fL[1]) + sl * pressureLR, den, rden);
+        real den = sl - sStar, rden = divI((real)1., den);
+        flux[0] = divByRecip(mulI(sStar, mulI(sl, stL[0]) - fL[0]), den, rden);
+        flux[1] = divByRecip(mulI(sStar, mulI(sl, stL[1]) - fL[1]) + mulI(sl, pressureLR), den, rden);
 #pragma unroll
-        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(sStar * (sl * stL[1 + k] - fL[1 + k]), den, rden);
-        flux[E] = divByRecip(sStar * (sl * stL[E] - fL[E]) + sl * pressureLR * sStar, den, rden);
+        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(mulI(sStar, mulI(sl, stL[1 + k]) - fL[1 + k]), den, rden);
+        flux[E] = divByRecip(mulI(sStar, mulI(sl, stL[E]) - fL[E]) + mulI(mulI(sl, pressureLR), sStar), den, rden);
     } else if (sStar <= (real)0. && (real)0. <= sr) {
-        real pressureLR = halfOf(L.pressure + R.pressure + L.density * (sl - L.v[0]) * (sStar - L.v[0]) +
-                                 R.density * (sr - R.v[0]) * (sStar - R.v[0]));
-        real den = sr - sStar, rden = (real)1. / den;
-        flux[0] = divByRecip(sStar * (sr * stR[0] - fR[0]), den, rden);
-        flux[1] = divByRecip(sStar * (sr * stR[1] - fR[1]) + sr * pressureLR, den, rden);
+        real pressureLR = halfOf(L.pressure + R.pressure + mulI(mulI(L.density, sl - L.v[0]), sStar - L.v[0]) +
+                                 mulI(mulI(R.density, sr - R.v[0]), sStar - R.v[0]));
+        real den = sr - sStar, rden = divI((real)1., den);
+        flux[0] = divByRecip(mulI(sStar, mulI(sr, stR[0]) - fR[0]), den, rden);
+        flux[1] = divByRecip(mulI(sStar, mulI(sr, stR[1]) - fR[1]) + mulI(sr, pressureLR), den, rden);
 #pragma unroll
-        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(sStar * (sr * stR[1 + k] - fR[1 + k]), den, rden);
-        flux[E] = divByRecip(sStar * (sr * stR[E] - fR[E]) + sr * pressureLR * sStar, den, rden);
+        for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(mulI(sStar, mulI(sr, stR[1 + k]) - fR[1 + k]), den, rden);
+        flux[E] = divByRecip(mulI(sStar, mulI(sr, stR[E]) - fR[E]) + mulI(mulI(sr, pressureLR), sStar), den, rden);
     } else if (sr <= (real)0.) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fR[i];
