@@ -26,6 +26,7 @@ SOURCES = {
     "kernels/probe.cu": ["--fmad=false"],
     "kernels/noalloc.cu": ["--fmad=false"],
     "kernels/batch.cu": ["--fmad=false"],
+    "kernels/batch_flux.cu": ["--fmad=false"],
     "kernels/adjoint.cu": [],
     "host/adjoint.cu": [],
     "host/batch_solver.cu": [],
@@ -33,7 +34,7 @@ SOURCES = {
     "host/capi.cu": [],
 }
 HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
-           "kernels/combine_cells.cuh", "kernels/batch.h", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",
+           "kernels/combine_cells.cuh", "kernels/batch.h", "kernels/batch_common.cuh", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",
            "kernels/adjoint.h", "host/adjoint.h"]
 
 

@@ -13,30 +13,10 @@
 #include "hllc_cells.cuh"
 #include "reduce.cuh"
 #include "roe_cells.cuh"
+#include "batch_common.cuh"
 
 namespace hgpu {
 namespace {
-
-// next work index for the whole block (all threads must call)
-__device__ __forceinline__ int nextItem(unsigned* q) {
-    __shared__ int item;
-    __syncthreads();
-    if (threadIdx.x == 0) item = (int)atomicAdd(q, 1u);
-    __syncthreads();
-    return item;
-}
-
-// the cell of this thread inside a tile, or false if outside the tile/grid
-__device__ __forceinline__ bool tileCell(const Grid& g, const BatchTile& t, const BatchTuning& tu, int& x, int& y, int& z,
-                                         long long& c) {
-    int tx = threadIdx.x % tu.tx, ty = (threadIdx.x / tu.tx) % tu.ty, tz = threadIdx.x / (tu.tx * tu.ty);
-    x = t.x0 + tx;
-    y = t.y0 + ty;
-    z = t.z0 + tz;
-    if (tz >= tu.tz || x >= g.S[0] || y >= g.S[1] || z >= g.S[2]) return false;
-    c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
-    return true;
-}
 
 // ghost fill of one problem per work item: every axis in order, lines in parallel
 template <typename real, int D>
@@ -146,32 +126,6 @@ __global__ void __launch_bounds__(256) batchDeltaQKernel(const BatchProblem<real
 }
 
 template <typename real, int D>
-__global__ void __launch_bounds__(256) batchFluxKernel(const BatchProblem<real>* __restrict__ P,
-                                                       const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
-                                                       int hllc, int lim, const StepConst<real>* __restrict__ sc,
-                                                       const real* __restrict__ stage, const real* __restrict__ faces,
-                                                       const real* __restrict__ dq, real* __restrict__ flux,
-                                                       unsigned* health, unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
-        const BatchTile tl = tiles[t];
-        const BatchProblem<real>& pr = P[tl.p];
-        int x, y, z;
-        long long c;
-        if (!tileCell(pr.g, tl, tu, x, y, z, c)) continue;
-        const real* st = stage + (long long)(D + 2) * pr.stateOff;
-        if (hllc) {
-            if (!hllcFluxCell<real, D>(pr.g, pr.ph, st, faces + pr.faceOff, flux + pr.dqOff, c, x, y, z))
-                atomicOr(health, HEALTH_HLLC_NOBRANCH);
-        } else {
-            roeFluxCell<real, D>(pr.g, lim, sc[tl.p], st, faces + pr.faceOff, dq + pr.dqOff, flux + pr.dqOff, c, x, y,
-                                 z);
-        }
-    }
-}
-
-template <typename real, int D>
 __global__ void __launch_bounds__(256) batchCombineKernel(const BatchProblem<real>* __restrict__ P,
                                                           const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                           const real* __restrict__ flux, CombinePlan<real> plan,
@@ -229,17 +183,6 @@ __global__ void __launch_bounds__(256) batchWaveKernel(const BatchProblem<real>*
     }
 }
 
-template <typename K>
-int persistentBlocks(K kernel, int smem, int perSM) {
-    int dev = 0, sms = 0, occ = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, smem);
-    if (occ < 1) occ = 1;
-    if (perSM > 0 && perSM < occ) occ = perSM;
-    return sms * occ;
-}
-
 }  // namespace
 
 template <typename real>
@@ -294,16 +237,6 @@ void BatchLaunch<real>::finalize(int integ, unsigned long long* acc, StepConst<r
 template <typename real>
 void BatchLaunch<real>::deltaQ(int loA, int hiA, const real* stage, real* dq, unsigned* q) const {
 #define L(DD) batchDeltaQKernel<real, DD><<<persistentBlocks(batchDeltaQKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, loA, hiA, stage, faces, dq, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
-#undef L
-}
-
-template <typename real>
-void BatchLaunch<real>::flux(int hllc, int lim, const StepConst<real>* sc, const real* stage, const real* dq,
-                             real* fluxBuf, unsigned* health, unsigned* q) const {
-#define L(DD) batchFluxKernel<real, DD><<<persistentBlocks(batchFluxKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, hllc, lim, sc, stage, faces, dq, fluxBuf, health, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);
