@@ -412,6 +412,13 @@ def adjoint_measure(hg, _abi, ic, args):
     }
 
 
+# DRAM bytes (read + write) per interior cell of one launch, from the ncu captures in
+# profiles/kernels_kh1024.md (KH 1024x1024, same kernels); traffic grows with the cells
+# processed, so the bench workload's per-launch traffic is this times its interior cells.
+MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 423.0, "roe_delta_q_tilde": 253.0, "roe_eigenbasis": 245.0,
+                             "flux_divergence_combine": 123.0}
+
+
 def run_gb300(args):
     rank, local_rank, world = dist_env()
     pg = None
@@ -474,10 +481,14 @@ def run_gb300(args):
     bytes_per_launch = algorithmic_bytes_per_cell(dom_name) * interior
     achieved_gbs = bytes_per_launch / (dom_ms * 1e-3) / 1e9
     fp64_peak = hg.fp64_peak()
+    traffic = MEASURED_TRAFFIC_PER_CELL.get(dom_name)
     roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind, "traffic": None,
+                "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind,
+                "traffic": traffic * interior if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 1024^2 "
+                                  "(profiles/kernels_kh1024.md), scaled by interior cells",
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": dom_ms,
-                "note": "FP64 issue rate, not HBM, bounds this kernel; see fp64"}
+                "note": "compute-bound (FP64 unit + integer pipes carrying binary64 products), not HBM-bound; see fp64"}
     breakdown = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / sum(x[1] for x in prof.values())}
                  for k, v in prof.items()}
 

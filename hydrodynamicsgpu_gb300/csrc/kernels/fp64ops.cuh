@@ -127,13 +127,23 @@ static __device__ __noinline__ double divNative(double x, double y) { return x /
 // v += v (2^126 - m_y 2^11 v) / 2^126; q is estimated as (m_x v) >> (63 - s), the
 // remainder r = m_x 2^(52+s) - q m_y is formed exactly modulo 2^64 (|r| < 2^63) and
 // q corrected until 0 <= r < m_y; then q is rounded up when 2r > m_y, or 2r = m_y
-// and q is odd.  Everything else takes the FP64 unit.  Checked against the FP64
-// unit's quotient on 4.3e9 random operand pairs.
+// and q is odd.  A zero operand beside a finite one is resolved with integer
+// operations; everything else takes the FP64 unit.  Checked against the FP64 unit's
+// quotient on 4.3e9 random operand pairs.
 __device__ __forceinline__ double divI(double x, double y) {
     const unsigned long long ux = (unsigned long long)bitsOf(x), uy = (unsigned long long)bitsOf(y);
     const unsigned ex = (unsigned)(ux >> 52) & 0x7FF, ey = (unsigned)(uy >> 52) & 0x7FF;
     int e = (int)ex - (int)ey + 1023;
-    if (ex - 1u >= 2046u || ey - 1u >= 2046u || (unsigned)(e - 2) >= 2044u) return divNative(x, y);
+    if (ex - 1u >= 2046u || ey - 1u >= 2046u || (unsigned)(e - 2) >= 2044u) {
+        // a zero operand beside a finite one: 0/0 = NaN, x/0 = +-Inf, 0/y = +-0 (the
+        // limiter ratios of flat states are mostly these); the rest on the FP64 unit
+        const bool xz = (ux << 1) == 0, yz = (uy << 1) == 0;
+        if ((xz || yz) && ex != 0x7FF && ey != 0x7FF) {
+            const unsigned long long sgn = (ux ^ uy) & 0x8000000000000000ull;
+            return fromBits((long long)(xz && yz ? 0x7FFFFFFFFFFFFFFFull : xz ? sgn : (sgn | 0x7FF0000000000000ull)));
+        }
+        return divNative(x, y);
+    }
     const unsigned long long mx = (ux & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const unsigned long long d = (uy & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const unsigned s = mx < d;

@@ -25,7 +25,8 @@ __device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
 }
 
 // operand classes: any exponent (zeros, subnormals, Inf/NaN included), moderate
-// exponents, short significands (exact products/quotients, powers of two), extremes
+// exponents, short significands (exact products/quotients, powers of two), extremes,
+// exact zeros / infinities / NaNs
 __device__ double operand(unsigned long long s, int cls) {
     const unsigned long long r = splitmix(s), m = r & 0xFFFFFFFFFFFFFull, sg = (r >> 63) << 63;
     const unsigned long long t = splitmix(s ^ 0x5bd1e995ull);
@@ -34,7 +35,8 @@ __device__ double operand(unsigned long long s, int cls) {
     if (cls == 0) e = (unsigned)(t % 2048);
     else if (cls == 1) e = 1023 - 60 + (unsigned)(t % 120);
     else if (cls == 2) { e = 1023 - 4 + (unsigned)(t % 8); mm = m & ~((1ull << (t >> 32) % 53) - 1); }
-    else e = (t & 1) ? (unsigned)(t % 40) : 2047 - (unsigned)(t % 40);
+    else if (cls == 3) e = (t & 1) ? (unsigned)(t % 40) : 2047 - (unsigned)(t % 40);
+    else { e = (t & 2) ? 0 : 2047; mm = (t & 4) ? 0 : (t & 8) ? mm : 1; }      // zeros, infinities, NaNs
     return fromBits((long long)(sg | ((unsigned long long)e << 52) | mm));
 }
 
@@ -43,7 +45,7 @@ __global__ void selftestKernel(unsigned long long seed, long long cases, unsigne
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cases;
          i += (long long)gridDim.x * blockDim.x) {
         const unsigned long long s = splitmix(seed + (unsigned long long)i);
-        const double x = operand(s, (int)(s % 4)), y = operand(s ^ 0xabcdefull, (int)((s >> 8) % 4));
+        const double x = operand(s, (int)(s % 5)), y = operand(s ^ 0xabcdefull, (int)((s >> 8) % 5));
         const double pm = x * y, qm = mulI(x, y), pd = x / y, qd = divI(x, y);
         if (bitsOf(pm) != bitsOf(qm) && !(pm != pm && qm != qm)) ++nm;
         if (bitsOf(pd) != bitsOf(qd) && !(pd != pd && qd != qd)) ++nd;
