@@ -104,7 +104,7 @@ __device__ __forceinline__ void loadParams(const double* __restrict__ B, long lo
     p.vv = 2. * p.hv2;
     p.c = .5 * (p.lamE - p.lam0);
     p.H = .5 * (p.hm + p.hp);
-    p.id = .5 / (p.c * p.c);
+    p.id = divI(.5, p.c * p.c);
 }
 
 // g.(L x): writes L^T g into gx and adds d(g.Lx)/d(vx, vt, c) into gp (H does not enter L)
@@ -179,7 +179,7 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
         lam[i] = i == 0 ? p.lam0 : (i == E ? p.lamE : p.vx);
         up[i] = geZero(lam[i]);
         const double theta = up[i] ? 1. : -1.;
-        rcp[i] = 1. / dq0[i];
+        rcp[i] = divI(1., dq0[i]);
         r[i] = divByRecip(up[i] ? dqM[i] : dqP[i], dq0[i], rcp[i]);
         Dual ph = limiterDual(lim, Dual{r[i], 1.});
         phi[i] = ph.v;
@@ -390,7 +390,7 @@ __device__ __forceinline__ void adjBasisFace(const Grid& g, const Phys<double>& 
     RoePrim<double, D> L, R;
     roePrim<double, D>(sL, ph.gamma, L);
     roePrim<double, D>(sR, ph.gamma, R);
-    const double norm = 1. / (L.w + R.w);
+    const double norm = divI(1., L.w + R.w);
     double v[3] = {0., 0., 0.}, vv = 0.;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -401,7 +401,7 @@ __device__ __forceinline__ void adjBasisFace(const Grid& g, const Phys<double>& 
     const double c0 = sqrt((H - .5 * vv) * gm1);
     const double* gP = S.gParam + (long long)SIDE * P * V + c;
     const double gc = gP[(D + 1) * V];
-    const double gcs = gc * gm1 * .5 / c0;            // dc/dH; dc/dv_k = -gcs v_k
+    const double gcs = divI(gc * gm1 * .5, c0);       // dc/dH; dc/dv_k = -gcs v_k
     double gv[3] = {0., 0., 0.};
     gv[SIDE] = gP[0];
     if (D > 1) gv[SIDE == 1 ? 0 : 1] = gP[1 * V];
@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(kT) adjPrimsKernel(Grid g, Phys<double> ph, co
     }
     if (!any) return;
     const double* s = U + (long long)N * c;
-    const double rho = s[0], ir = 1. / rho, gm1 = ph.gamma - 1.;
+    const double rho = s[0], ir = divI(1., rho), gm1 = ph.gamma - 1.;
     double v[3], vv = 0.;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(kT) adjPrimsKernel(Grid g, Phys<double> ph, co
         l[1 + k] += (gp[k] - gh * gm1 * v[k]) * ir;
     }
     l[E] += gh * ph.gamma * ir;
-    l[0] += grho * ir + gw * .5 / sqrt(rho);
+    l[0] += grho * ir + divI(gw * .5, sqrt(rho));
 }
 
 // transposed ghost fill of one line along `axis` (boundaryLine run backwards)
