@@ -481,6 +481,8 @@ void HLL<real>::calcTimestep() {                             // HLL::calcTimeste
 template <typename real>
 void HLL<real>::step() {                                     // HLL::step (HLL.cpp:40-47)
     this->integrator->integrate([this](real* stage) {
+        // SEAM: the stage's ghosts are refreshed, so both periodic seam faces see the same cells
+        if (this->rc.cfg.compat == HGPU_COMPAT_SEAM && stage != this->state.template as<real>()) this->boundaryOn(stage);
         this->launch("hllc_flux", 1, [&] {
             launchHllcFlux<real>(this->rc.grid, this->ph, stage, waves.template as<real>(),
                                  this->flux.template as<real>(), this->health, this->stream);

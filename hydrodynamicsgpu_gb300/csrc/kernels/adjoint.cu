@@ -186,7 +186,7 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
         dphi[i] = ph.d;
         em[i] = lam[i] * k - theta;
         A[i] = theta + phi[i] * em[i];
-        ft[i] = lam[i] * y[i] - .5 * lam[i] * dq0[i] * A[i];
+        ft[i] = lam[i] * (y[i] - .5 * dq0[i] * A[i]);
     }
     // reverse through F = R ft
     double gft[N], gp[P];
@@ -212,13 +212,15 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
     double gy[N], gq0[N], gqM[N], gqP[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-        const double gf = gft[i];
-        gy[i] = lam[i] * gf;
-        const double gLam = gf * (y[i] - .5 * dq0[i] * A[i] - .5 * lam[i] * dq0[i] * phi[i] * k);
-        gq0[i] = -.5 * lam[i] * A[i] * gf;
+        // ft_i = lam (y - h A), h = dq0 / 2, A = theta + phi (lam k - theta):
+        // d/dlam = y - h A - h lam phi k,  d/ddq0 = -lam A / 2,  d/dphi = -h lam (lam k - theta)
+        const double gf = gft[i], t = lam[i] * gf, h = .5 * dq0[i];
+        gy[i] = t;
+        const double gLam = gf * y[i] - h * (A[i] * gf + phi[i] * k * t);
+        gq0[i] = -.5 * A[i] * t;
         gqM[i] = 0.;
         gqP[i] = 0.;
-        const double gphi = -.5 * lam[i] * dq0[i] * em[i] * gf;
+        const double gphi = -h * em[i] * t;
         if (dphi[i] != 0. && isfinite(dphi[i]) && isfinite(r[i])) {
             const double gr = gphi * dphi[i];
             const double gUp = gr * rcp[i];
