@@ -339,6 +339,35 @@ def fd_stats(pairs):
             "within_1e-6": int((err <= 1e-6).sum())}
 
 
+def fp32_measure(hg, _abi, ic, args):
+    """FP32 instantiation: the KH workload's throughput, and its error against FP64
+    after 100 steps on KH 512^2 (each precision with its own CFL dt), per conserved
+    variable as max |u32 - u64| / max |u64|."""
+    size = args.size
+    cfg = _abi.make_config(solver="EulerRoe", size=(size, size), boundary="PERIODIC", limiter="MinMod",
+                           integrator="RungeKutta4", precision=_abi.FP32)
+    s_ = hg.Solver(cfg)
+    s_.resetState(ic.kelvin_helmholtz(size=(size, size), seed=0).astype(np.float32))
+    s_.update(args.warmup, want_dt=False)
+    ms = s_.timed_update(args.steps) / args.steps
+    s_.close()
+    n = 512
+    u0 = ic.kelvin_helmholtz(size=(n, n), seed=0).reshape(-1)
+    out = {}
+    for prec in (_abi.FP64, _abi.FP32):
+        c = _abi.make_config(solver="EulerRoe", size=(n, n), boundary="PERIODIC", limiter="MinMod",
+                             integrator="RungeKutta4", precision=prec)
+        s_ = hg.Solver(c)
+        s_.resetState(u0.astype(np.float32) if prec == _abi.FP32 else u0)
+        s_.update(100, want_dt=False)
+        out[prec] = s_.getState().astype(np.float64).reshape(-1, N_STATES)
+        s_.close()
+    err = np.max(np.abs(out[_abi.FP32] - out[_abi.FP64]), axis=0) / np.max(np.abs(out[_abi.FP64]), axis=0)
+    return {"value": (size - 4) ** 2 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+            "error_vs_fp64_100_steps_512": {"rho": float(err[0]), "mx": float(err[1]), "my": float(err[2]),
+                                            "E": float(err[3])}}
+
+
 def adjoint_measure(hg, _abi, ic, args):
     """Adjoint workload: Kelvin-Helmholtz 512^2 problems (seeds 100..), EulerRoe FP64
     RK2 MinMod periodic, `adjoint_steps` steps with CFL dt recorded and then frozen,
@@ -533,7 +562,9 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_sample(size)
 
-    batched = adjoint = None
+    batched = adjoint = fp32 = None
+    if rank == 0 and world == 1:
+        fp32 = fp32_measure(hg, _abi, ic, args)
     if rank == 0 and world == 1 and not args.no_batch:
         batched = batched_sweep(hg, _abi, ic, args)
     if rank == 0 and world == 1 and not args.no_adjoint:
@@ -553,6 +584,7 @@ def run_gb300(args):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
+        "fp32": fp32,
         "batched_sweep": batched,
         "adjoint": adjoint,
         "gpu_launches": kernels_per_step * args.steps,
