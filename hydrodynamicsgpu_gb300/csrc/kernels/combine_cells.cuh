@@ -105,7 +105,7 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
 #pragma unroll
             for (int j = 0; j < N; ++j) {
                 const real* f = flux + ((long long)side * N + j) * g.V + c;
-                real t = divByRecip(f[g.step[side]] - f[0], ph.dx[side], ph.rdx[side]);   // deltaFlux / dx[side]
+                real t = divI(f[g.step[side]] - f[0], ph.dx[side]);   // deltaFlux / dx[side]
                 d[j] = side == 0 ? zfix(-t) : d[j] - t;
             }
         }

@@ -264,7 +264,7 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
     const real vx = rec[R_::VX];
     const bool midUp = geZero(vx);
     const real midTheta = midUp ? (real)1. : (real)-1.;
-    const real midEps = vx * dt_dx;
+    const real midEps = mulI(vx, dt_dx);
     const real midEpsTheta = midEps - midTheta;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -275,11 +275,11 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
         real rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
         real theta = mid ? midTheta : (up ? (real)1. : (real)-1.);
         real phi = slopeLimiter<real>(LIM >= 0 ? LIM : lim, rTilde);
-        real epsMinusTheta = mid ? midEpsTheta : eigenvalue * dt_dx - theta;
-        real deltaFluxTilde = eigenvalue * dq[i];
+        real epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
+        real deltaFluxTilde = mulI(eigenvalue, dq[i]);
         // `fluxTilde[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta))`
-        // (the per-wave products stay on the FP64 unit: they lie on the critical path
-        // between the two transforms, whose products run on the integer pipes)
+        // (the products on the path from L*avg to R*ft stay on the FP64 unit; eps and
+        // lambda*dq, off that path, run on the integer pipes like the transforms)
         if (sizeof(real) == 8) ft[i] = ft[i] - halfOf(deltaFluxTilde) * (theta + phi * epsMinusTheta);
         else ft[i] -= .5 * deltaFluxTilde * (theta + phi * epsMinusTheta);   // double literal: FP32 promotes
     }
