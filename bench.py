@@ -458,12 +458,9 @@ MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 423.0, "roe_delta_q_tilde": 253.0, "roe
 
 
 def run_gb300(args):
-    rank, local_rank, world = dist_env()
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        pg = dist
+    from hydrodynamicsgpu_gb300.replicas import Replicas
+    reps = Replicas()
+    rank, local_rank, world = reps.rank, reps.local_rank, reps.world
     import hydrodynamicsgpu_gb300 as hg
     from hydrodynamicsgpu_gb300 import _abi, initconds as ic
     if not os.path.exists(hg.LIB_PATH):
@@ -478,17 +475,8 @@ def run_gb300(args):
     solver.resetState(init)
     interior = (size - 4) * (size - 4)
 
-    def barrier():
-        if pg:
-            pg.barrier()
-
-    def max_over_ranks(x):
-        if not pg:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
+    barrier = reps.barrier
+    max_over_ranks = reps.max
 
     # warm-up (also captures the CUDA graph of one step)
     solver.update(args.warmup, want_dt=False)
@@ -593,8 +581,7 @@ def run_gb300(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()
-    if pg:
-        pg.destroy_process_group()
+    reps.close()
     return 0
 
 
