@@ -32,6 +32,7 @@ SIGNATURES = {
     "hgpu_set_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     "hgpu_get_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     "hgpu_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_step": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_last_dt": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_synchronize": (ctypes.c_int, [_P]),
     "hgpu_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
@@ -63,6 +64,7 @@ SIGNATURES = {
     "hgpu_batch_set_state": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t]),
     "hgpu_batch_get_state": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t]),
     "hgpu_batch_update": (ctypes.c_int, [_P, ctypes.c_int]),
+    "hgpu_batch_step": (ctypes.c_int, [_P, ctypes.c_int]),
     "hgpu_batch_timed_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "hgpu_batch_dts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "hgpu_batch_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),

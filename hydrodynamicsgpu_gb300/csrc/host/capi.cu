@@ -187,6 +187,8 @@ int hgpu_update(hgpu_solver* h, int nsteps, double* last_dt) {
     });
 }
 
+int hgpu_step(hgpu_solver* h, int nsteps, double* last_dt) { return hgpu_update(h, nsteps, last_dt); }
+
 int hgpu_last_dt(hgpu_solver* h, double* dt) {
     if (!h || !dt) return fail(HGPU_ERR_ARG, "null argument");
     return guarded([&]() { *dt = h->s->lastDt(); return (int)HGPU_OK; });
@@ -454,6 +456,8 @@ int hgpu_batch_update(hgpu_batch* b, int nsteps) {
     if (!b || nsteps < 0) return fail(HGPU_ERR_ARG, "bad argument");
     return guarded([&]() { b->b->run(nsteps); return (int)HGPU_OK; });
 }
+
+int hgpu_batch_step(hgpu_batch* b, int nsteps) { return hgpu_batch_update(b, nsteps); }
 
 int hgpu_batch_timed_update(hgpu_batch* b, int nsteps, float* ms) {
     if (!b || !ms || nsteps < 0) return fail(HGPU_ERR_ARG, "bad argument");

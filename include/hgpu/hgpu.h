@@ -178,6 +178,8 @@ int hgpu_get_state(hgpu_solver* s, void* host_state, size_t count);
  * the call returns after the last step's work is queued and, if last_dt is
  * non-NULL, after it finished, with that step's dt.  */
 int hgpu_update(hgpu_solver* s, int nsteps, double* last_dt);
+/* The same call under the name a step-oriented binding uses. */
+int hgpu_step(hgpu_solver* s, int nsteps, double* last_dt);
 
 /* dt of the most recent step (blocks on the solver's stream). */
 int hgpu_last_dt(hgpu_solver* s, double* dt);
@@ -248,6 +250,8 @@ int hgpu_batch_set_state(hgpu_batch* b, int problem, const void* host_state, siz
 int hgpu_batch_get_state(hgpu_batch* b, int problem, void* host_state, size_t count);
 /* Advance every problem nsteps Solver::update steps (graph replays; returns when queued). */
 int hgpu_batch_update(hgpu_batch* b, int nsteps);
+/* The same call under the name a step-oriented binding uses. */
+int hgpu_batch_step(hgpu_batch* b, int nsteps);
 /* Same, returning the device time of the nsteps in milliseconds (CUDA events). */
 int hgpu_batch_timed_update(hgpu_batch* b, int nsteps, float* ms);
 /* dt of the most recent step of every problem (n = number of problems). */

@@ -160,3 +160,27 @@ def test_multi_step_call_matches_single_steps(hg, oracle_mod):
     assert a.last_dt() == b.last_dt()
     a.close()
     b.close()
+
+
+def test_step_aliases_match_update(hg):
+    """hgpu_step / hgpu_batch_step are hgpu_update / hgpu_batch_update."""
+    import ctypes
+    cfg = _abi.make_config(solver="EulerRoe", size=SMALL[2], boundary="PERIODIC", limiter="Superbee",
+                           integrator="RungeKutta2")
+    init = random_state(cfg, seed=8)
+    a, b = hg.Solver(cfg), hg.Solver(cfg)
+    a.resetState(init)
+    b.resetState(init)
+    a.update(3)
+    dt = ctypes.c_double()
+    hg.check(hg.lib().hgpu_step(b.h, 3, ctypes.byref(dt)))
+    assert same(a.getState(), b.getState()) and dt.value == a.last_dt()
+    ba, bb = hg.Batch([cfg, cfg]), hg.Batch([cfg, cfg])
+    for bt in (ba, bb):
+        bt.set_state(0, init)
+        bt.set_state(1, init)
+    ba.update(2)
+    hg.check(hg.lib().hgpu_batch_step(bb.h, 2))
+    assert same(ba.get_state(1), bb.get_state(1))
+    for x in (a, b, ba, bb):
+        x.close()
