@@ -61,13 +61,14 @@ RoeAdjoint::Tape RoeAdjoint::makeTape() const {
     for (int k = 0; k < stages_; ++k) {
         t.U.emplace_back(sizeof(double) * V * N, false);
         t.DQ.emplace_back(sizeof(double) * V * N * D, true);
+        t.FT.emplace_back(sizeof(double) * V * roeFluxTapePlanes((int)D), false);
     }
     return t;
 }
 
 size_t RoeAdjoint::tapeBytes() const {
     const size_t V = (size_t)rc_.grid.V, N = rc_.numStates, D = rc_.dim;
-    return sizeof(double) * V * (D * roeRecordSize((int)D) + stages_ * (N + N * D));
+    return sizeof(double) * V * (D * roeRecordSize((int)D) + stages_ * (N + N * D + roeFluxTapePlanes((int)D)));
 }
 
 void RoeAdjoint::forward(const double* u_n, double dt, Tape& t, double* u_next) {
@@ -82,8 +83,8 @@ void RoeAdjoint::forward(const double* u_n, double dt, Tape& t, double* u_next) 
     auto stage = [&](int k, const double* in) {
         cudaCheck(cudaMemcpyAsync(t.U[k].get(), in, bytes, cudaMemcpyDeviceToDevice, stream_), "tape stage");
         launchRoeDeltaQ<double>(g, in, t.basis.as<double>(), t.DQ[k].as<double>(), 0, stream_);
-        launchRoeFlux<double>(g, rc_.cfg.limiter, in, t.basis.as<double>(), t.DQ[k].as<double>(), sc,
-                              flux_.as<double>(), 0, stream_);
+        launchRoeFluxRecord(g, rc_.cfg.limiter, in, t.basis.as<double>(), t.DQ[k].as<double>(), sc,
+                            flux_.as<double>(), t.FT[k].as<double>(), stream_);
     };
     if (fe_) {
         stage(0, cur);
@@ -129,8 +130,8 @@ void RoeAdjoint::reverse(const Tape& t, double dt, const double* lamNext, double
             st.coefF[i] = (fe_ ? 1. : tableauBeta(integ_, m - 1, k)) * dt;
         }
         const double* U = t.U[k].as<double>();
-        launchAdjFlux(g, ph_, rc_.cfg.limiter, dtdx, U, t.DQ[k].as<double>(), t.basis.as<double>(), st, S_,
-                      k == stages_ - 1, stream_);
+        launchAdjFlux(g, ph_, rc_.cfg.limiter, dtdx, U, t.DQ[k].as<double>(), t.basis.as<double>(),
+                      t.FT[k].as<double>(), st, S_, k == stages_ - 1, stream_);
         launchAdjDeltaQ(g, ph_, U, t.basis.as<double>(), S_, stream_);
         launchAdjCells(g, st, S_, k == 0 ? lamOut : lams_[k - 1].as<double>(), stream_);
     }

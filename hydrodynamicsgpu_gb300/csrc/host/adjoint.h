@@ -18,6 +18,7 @@ public:
     struct Tape {
         DeviceBuffer basis;                  // eigenbasis of u_0 (compact records)
         std::vector<DeviceBuffer> U, DQ;     // stage inputs u_k (u_0 = ghost-filled u^n) and their Delta-q-tilde
+        std::vector<DeviceBuffer> FT;        // per stage: the flux's per-wave values (roe_record.cu)
     };
     RoeAdjoint(const ResolvedConfig& rc, cudaStream_t stream);
     Tape makeTape() const;

@@ -18,69 +18,13 @@
 #include "common.cuh"
 #include "roe.cuh"
 #include "roe_cells.cuh"
+#include "limiter_dual.cuh"
 
 namespace hgpu {
 namespace {
 
 constexpr int kT = 256;
 inline unsigned blocksFor(long long n) { return (unsigned)((n + kT - 1) / kT); }
-
-// ---- limiter value and derivative along the forward's branch ----
-struct Dual {
-    double v, d;
-};
-__device__ __forceinline__ Dual cst(double c) { return {c, 0.}; }
-__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
-__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
-__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
-__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
-    double q = a.v / b.v;
-    return {q, (a.d - q * b.d) / b.v};
-}
-__device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
-__device__ __forceinline__ Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
-__device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
-__device__ __forceinline__ Dual operator/(double a, Dual b) { return cst(a) / b; }
-__device__ __forceinline__ Dual dabs(Dual a) { return signbit(a.v) ? Dual{-a.v, -a.d} : a; }
-// the operand fminLibm / fmaxLibm return: NaN yields the other, ties the second
-__device__ __forceinline__ Dual dmin(Dual a, Dual b) {
-    if (b.v != b.v) return a;
-    if (a.v != a.v) return b;
-    return a.v < b.v ? a : b;
-}
-__device__ __forceinline__ Dual dmax(Dual a, Dual b) {
-    if (b.v != b.v) return a;
-    if (a.v != a.v) return b;
-    return a.v > b.v ? a : b;
-}
-
-// res/SlopeLimiter.cl, same expressions and min/max operand order as slopeLimiter()
-__device__ __forceinline__ Dual limiterDual(int lim, Dual r) {
-    const Dual z = cst(0.), one = cst(1.);
-    switch (lim) {
-    case 0: return z;
-    case 1: return one;
-    case 2: return r;
-    case 3: return .5 * (1. + r);
-    case 4: return dmax(z, r) * (3. * r + 1.) / ((r + 1.) * (r + 1.));
-    case 5: return dmax(z, 1.5 * (r + dabs(r)) / (r + 2.));
-    case 6: return dmax(z, 2. * (r + dabs(r)) / (r + 3.));
-    case 7: return dmax(z, dmin(2. * r, dmin((1. + 2. * r) / cst(3.), cst(2.))));
-    case 8: return dmax(z, dmin(r, one));
-    case 9: return dmax(z, dmin(r, cst(1.5)));
-    case 10: return .5 * (r * r + r) / ((r * r + r) + 1.);
-    case 11: return dmax(z, dmin(2. * r, dmin(.25 + .75 * r, cst(4.))));
-    case 12: return dmax(z, dmax(dmin(1.5 * r, one), dmin(r, cst(1.5))));
-    case 13: return dmax(z, dmin(dmin(2. * r, .75 + .25 * r), dmin(.25 + .75 * r, cst(2.))));
-    case 14: return (r * r + r) / (r * r + 1.);
-    case 15: return 2. * r / (r * r + 1.);
-    case 16: return dmax(z, r) * cst(2.) / (1. + r);
-    case 17: return dmax(z, dmin(cst(2.), dmin(.5 * (1. + r), 2. * r)));
-    case 18: return dmax(z, dmax(dmin(one, 2. * r), dmin(cst(2.), r)));
-    case 19: return .5 * (r + 1.) * dmin(one, dmin(4. * r / (r + 1.), 4. / (r + 1.)));
-    }
-    return z;
-}
 
 // face parameters from the compact record (normal frame)
 template <int D>
@@ -134,60 +78,31 @@ __device__ __forceinline__ void leftVJP(const FaceParams<D>& p, double gm1, cons
     gp[D + 1] -= (2. * a * Q + b * W) * (2. * p.c * p.id);   // / c
 }
 
-// one face of the flux VJP (stage k): gn = cotangent of the face flux (global frame)
+// one face of the flux VJP (stage k): gn = cotangent of the face flux (global frame).
+// The forward's per-wave values (L avg, A, phi, phi', r, ft) come from the recording
+// forward's tape (roe_record.cu).
 template <int D, int SIDE>
 __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, double k,
                                             const double* __restrict__ U, const double* __restrict__ DQ,
-                                            const double* __restrict__ B, const double* gFc, const double* gFl,
-                                            double rdx, const AdjScratch& S, int first, long long c) {
+                                            const double* __restrict__ B, const double* __restrict__ FT,
+                                            const double* gFc, const double* gFl, double rdx, const AdjScratch& S,
+                                            int first, long long c) {
     const int N = D + 2, E = N - 1, P = D + 2;
     const long long V = g.V, st = g.step[SIDE];
+    (void)lim;
     FaceParams<D> p;
     loadParams<D>(B, V, SIDE, c, p);
-    double gn[N], avg[N], dq0[N], dqM[N], dqP[N];
+    double gn[N], avg[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) {
         const int pj = perm<SIDE>(j);
         gn[j] = (gFc[pj] - gFl[pj]) * rdx;
         avg[j] = .5 * (U[N * (c - st) + pj] + U[N * c + pj]);
     }
+    const double* T = FT + (long long)SIDE * FT_PLANES * N * V + c;
+    double ft[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-        const double* q = DQ + ((long long)SIDE * N + i) * V + c;
-        dqM[i] = q[-st];
-        dq0[i] = q[0];
-        dqP[i] = q[st];
-    }
-    // forward: y = L avg, wave quantities, ft
-    double y[N];
-    {
-        double vtx = 0.;
-#pragma unroll
-        for (int t = 0; t < D - 1; ++t) vtx += p.vt[t] * avg[2 + t];
-        const double Q = gm1 * (.5 * p.vv * avg[0] - p.vx * avg[1] - vtx + avg[E]);
-        const double W = p.vx * avg[0] - avg[1];
-        y[0] = (Q + p.c * W) * p.id;
-        y[1] = avg[0] - 2. * Q * p.id;
-#pragma unroll
-        for (int t = 0; t < D - 1; ++t) y[2 + t] = avg[2 + t] - p.vt[t] * avg[0];
-        y[E] = (Q - p.c * W) * p.id;
-    }
-    double lam[N], A[N], phi[N], dphi[N], r[N], rcp[N], em[N], ft[N];
-    bool up[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        lam[i] = i == 0 ? p.lam0 : (i == E ? p.lamE : p.vx);
-        up[i] = geZero(lam[i]);
-        const double theta = up[i] ? 1. : -1.;
-        rcp[i] = divI(1., dq0[i]);
-        r[i] = divByRecip(up[i] ? dqM[i] : dqP[i], dq0[i], rcp[i]);
-        Dual ph = limiterDual(lim, Dual{r[i], 1.});
-        phi[i] = ph.v;
-        dphi[i] = ph.d;
-        em[i] = lam[i] * k - theta;
-        A[i] = theta + phi[i] * em[i];
-        ft[i] = lam[i] * (y[i] - .5 * dq0[i] * A[i]);
-    }
+    for (int i = 0; i < N; ++i) ft[i] = T[((long long)FT_F * N + i) * V];
     // reverse through F = R ft
     double gft[N], gp[P];
 #pragma unroll
@@ -214,19 +129,27 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
     for (int i = 0; i < N; ++i) {
         // ft_i = lam (y - h A), h = dq0 / 2, A = theta + phi (lam k - theta):
         // d/dlam = y - h A - h lam phi k,  d/ddq0 = -lam A / 2,  d/dphi = -h lam (lam k - theta)
-        const double gf = gft[i], t = lam[i] * gf, h = .5 * dq0[i];
+        const double lam = i == 0 ? p.lam0 : (i == E ? p.lamE : p.vx);
+        const bool up = geZero(lam);
+        const double em = lam * k - (up ? 1. : -1.);
+        const double dq0 = DQ[((long long)SIDE * N + i) * V + c];
+        const double y = T[((long long)FT_Y * N + i) * V], A = T[((long long)FT_A * N + i) * V];
+        const double phi = T[((long long)FT_PHI * N + i) * V], dphi = T[((long long)FT_DPHI * N + i) * V];
+        const double gf = gft[i], t = lam * gf, h = .5 * dq0;
         gy[i] = t;
-        const double gLam = gf * y[i] - h * (A[i] * gf + phi[i] * k * t);
-        gq0[i] = -.5 * A[i] * t;
+        const double gLam = gf * y - h * (A * gf + phi * k * t);
+        gq0[i] = -.5 * A * t;
         gqM[i] = 0.;
         gqP[i] = 0.;
-        const double gphi = -h * em[i] * t;
-        if (dphi[i] != 0. && isfinite(dphi[i]) && isfinite(r[i])) {
-            const double gr = gphi * dphi[i];
-            const double gUp = gr * rcp[i];
-            gq0[i] -= gUp * r[i];
-            if (up[i]) gqM[i] = gUp;
-            else gqP[i] = gUp;
+        const double gphi = -h * em * t;
+        if (dphi != 0. && isfinite(dphi)) {
+            const double r = T[((long long)FT_R * N + i) * V];
+            if (isfinite(r)) {
+                const double gUp = gphi * dphi * divI(1., dq0);
+                gq0[i] -= gUp * r;
+                if (up) gqM[i] = gUp;
+                else gqP[i] = gUp;
+            }
         }
         gp[0] += gLam;
         if (i == 0) gp[D + 1] -= gLam;
@@ -268,8 +191,8 @@ __device__ __forceinline__ void stageCotangent(const AdjStage& st, long long c, 
 template <int D>
 __global__ void __launch_bounds__(kT) adjFluxKernel(Grid g, Phys<double> ph, int lim, double k0, double k1, double k2,
                                                     const double* __restrict__ U, const double* __restrict__ DQ,
-                                                    const double* __restrict__ B, AdjStage st, AdjScratch S,
-                                                    int first) {
+                                                    const double* __restrict__ B, const double* __restrict__ FT,
+                                                    AdjStage st, AdjScratch S, int first) {
     const int N = D + 2;
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
@@ -288,11 +211,11 @@ __global__ void __launch_bounds__(kT) adjFluxKernel(Grid g, Phys<double> ph, int
         double gFl[N];
         stageCotangent<N>(st, c - g.step[side], inRange(g, cl[0], cl[1], cl[2], 2, 2), gFl);
         if (side == 0)
-            adjFluxFace<D, 0>(g, gm1, lim, ks[0], U, DQ, B, gFc, gFl, ph.rdx[0], S, first, c);
+            adjFluxFace<D, 0>(g, gm1, lim, ks[0], U, DQ, B, FT, gFc, gFl, ph.rdx[0], S, first, c);
         else if (side == 1)
-            adjFluxFace<D, (D > 1 ? 1 : 0)>(g, gm1, lim, ks[1], U, DQ, B, gFc, gFl, ph.rdx[1], S, first, c);
+            adjFluxFace<D, (D > 1 ? 1 : 0)>(g, gm1, lim, ks[1], U, DQ, B, FT, gFc, gFl, ph.rdx[1], S, first, c);
         else
-            adjFluxFace<D, (D > 2 ? 2 : 0)>(g, gm1, lim, ks[2], U, DQ, B, gFc, gFl, ph.rdx[2], S, first, c);
+            adjFluxFace<D, (D > 2 ? 2 : 0)>(g, gm1, lim, ks[2], U, DQ, B, FT, gFc, gFl, ph.rdx[2], S, first, c);
     }
 }
 
@@ -537,9 +460,9 @@ __global__ void adjBoundaryKernel(Grid g, int axis, int N, int mMin, int mMax, d
 }  // namespace
 
 void launchAdjFlux(const Grid& g, const Phys<double>& ph, int limiter, const double* dtdx, const double* stage,
-                   const double* dq, const double* basis, const AdjStage& st, const AdjScratch& s, int first,
-                   cudaStream_t stream) {
-#define L(DD) adjFluxKernel<DD><<<blocksFor(g.V), kT, 0, stream>>>(g, ph, limiter, dtdx[0], dtdx[1], dtdx[2], stage, dq, basis, st, s, first)
+                   const double* dq, const double* basis, const double* fluxTape, const AdjStage& st,
+                   const AdjScratch& s, int first, cudaStream_t stream) {
+#define L(DD) adjFluxKernel<DD><<<blocksFor(g.V), kT, 0, stream>>>(g, ph, limiter, dtdx[0], dtdx[1], dtdx[2], stage, dq, basis, fluxTape, st, s, first)
     if (g.dim == 1) L(1);
     else if (g.dim == 2) L(2);
     else L(3);

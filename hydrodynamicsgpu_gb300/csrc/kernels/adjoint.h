@@ -37,9 +37,15 @@ struct AdjScratch {
     double* gPrimR;   // D+2 per face: (v..., h, w) of the right cell
 };
 
+// the forward flux that also records the per-wave values the flux VJP reads
+// (roe_record.cu); roeFluxTapePlanes(dim) planes of V values
+int roeFluxTapePlanes(int dim);
+void launchRoeFluxRecord(const Grid& g, int limiter, const double* stage, const double* basis, const double* dq,
+                         const StepConst<double>* sc, double* flux, double* tape, cudaStream_t st);
+
 void launchAdjFlux(const Grid& g, const Phys<double>& ph, int limiter, const double* dtdx, const double* stage,
-                   const double* dq, const double* basis, const AdjStage& st, const AdjScratch& s, int first,
-                   cudaStream_t stream);
+                   const double* dq, const double* basis, const double* fluxTape, const AdjStage& st,
+                   const AdjScratch& s, int first, cudaStream_t stream);
 void launchAdjDeltaQ(const Grid& g, const Phys<double>& ph, const double* stage, const double* basis,
                      const AdjScratch& s, cudaStream_t stream);
 void launchAdjCells(const Grid& g, const AdjStage& st, const AdjScratch& s, double* lamOut, cudaStream_t stream);

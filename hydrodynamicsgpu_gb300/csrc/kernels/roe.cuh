@@ -13,6 +13,7 @@
 #pragma once
 #include "common.cuh"
 #include "fp64ops.cuh"
+#include "limiter_dual.cuh"
 
 namespace hgpu {
 
@@ -249,11 +250,17 @@ __device__ __forceinline__ real roeEigenvalue(const real* rec, int i) {
 
 // Limited characteristic flux of one interface (res/Roe.cl:253-298).
 // sL, sR: stage states; dqL, dq, dqR: Delta-q-tilde at the faces before/at/after.
+// Per-wave values the adjoint reads back from a recording forward (REC): plane q of
+// wave i of a face at tape[(q N + i) V] (the caller offsets tape to the face).
+enum { FT_Y = 0, FT_A = 1, FT_PHI = 2, FT_DPHI = 3, FT_R = 4, FT_F = 5, FT_PLANES = 6 };
+
 // LIM >= 0 fixes the slope limiter at compile time (the kernel then carries one
 // limiter instead of all twenty at each of its wave sites); -1 dispatches on `lim`.
-template <typename real, int D, int SIDE, int LIM = -1>
+// REC (FP64 only) also stores the per-wave values above; the flux is the same.
+template <typename real, int D, int SIDE, int LIM = -1, bool REC = false>
 __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const real* sR, const real* dqL,
-                                        const real* dq, const real* dqR, real dt_dx, int lim, real* F) {
+                                        const real* dq, const real* dqR, real dt_dx, int lim, real* F,
+                                        real* __restrict__ tape = nullptr, long long V = 0) {
     typedef RoeRec<D> R_;
     const int N = D + 2;
     real avg[5], ft[5];
@@ -270,6 +277,7 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
     for (int i = 0; i < N; ++i) {
         const bool mid = i > 0 && i < N - 1;
         real eigenvalue = roeEigenvalue<real, D>(rec, i);
+        if (REC) tape[((long long)FT_Y * N + i) * V] = ft[i];
         ft[i] = ft[i] * eigenvalue;
         bool up = mid ? midUp : geZero(eigenvalue);
         real rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
@@ -280,7 +288,17 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
         // `fluxTilde[i] -= .5 * deltaFluxTilde * (theta + phi * (epsilon - theta))`
         // (the products on the path from L*avg to R*ft stay on the FP64 unit; eps and
         // lambda*dq, off that path, run on the integer pipes like the transforms)
-        if (sizeof(real) == 8) ft[i] = ft[i] - halfOf(deltaFluxTilde) * (theta + phi * epsMinusTheta);
+        if (sizeof(real) == 8) {
+            const real A = theta + phi * epsMinusTheta;
+            ft[i] = ft[i] - halfOf(deltaFluxTilde) * A;
+            if (REC) {
+                tape[((long long)FT_A * N + i) * V] = A;
+                tape[((long long)FT_PHI * N + i) * V] = phi;
+                tape[((long long)FT_DPHI * N + i) * V] = limiterDual(LIM >= 0 ? LIM : lim, Dual{(double)rTilde, 1.}).d;
+                tape[((long long)FT_R * N + i) * V] = rTilde;
+                tape[((long long)FT_F * N + i) * V] = ft[i];
+            }
+        }
         else ft[i] -= .5 * deltaFluxTilde * (theta + phi * epsMinusTheta);   // double literal: FP32 promotes
     }
     rightTransform<real, D, SIDE>(rec, ft, F);

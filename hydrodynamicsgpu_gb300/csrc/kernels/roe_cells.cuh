@@ -124,10 +124,11 @@ __device__ __forceinline__ void roeDeltaQCell(const Grid& g, const real* __restr
     if (D > 2 && roeFace(g, 2, x, y, z, loA, hiA)) deltaQFace<real, D, (D > 2 ? 2 : 0)>(g, stage, basis, dq, c, sR);
 }
 
-template <typename real, int D, int SIDE, int LIM = -1>
+template <typename real, int D, int SIDE, int LIM = -1, bool REC = false>
 __device__ __forceinline__ void fluxFace(const Grid& g, int lim, real dt_dx, const real* __restrict__ stage,
                                          const real* __restrict__ basis, const real* __restrict__ dq,
-                                         real* __restrict__ flux, long long c, const real* sR) {
+                                         real* __restrict__ flux, long long c, const real* sR,
+                                         real* __restrict__ tape = nullptr) {
     const int N = D + 2, NB = RoeRec<D>::NB;
     real sL[N], rec[NB], qL[N], q[N], qR[N], F[N];
     const long long st = g.step[SIDE];
@@ -141,24 +142,26 @@ __device__ __forceinline__ void fluxFace(const Grid& g, int lim, real dt_dx, con
         q[i] = p[0];
         qR[i] = p[st];
     }
-    roeFlux<real, D, SIDE, LIM>(rec, sL, sR, qL, q, qR, dt_dx, lim, F);
+    roeFlux<real, D, SIDE, LIM, REC>(rec, sL, sR, qL, q, qR, dt_dx, lim, F,
+                                     REC ? tape + (long long)SIDE * FT_PLANES * N * g.V + c : nullptr, g.V);
 #pragma unroll
     for (int j = 0; j < N; ++j) flux[((long long)SIDE * N + j) * g.V + c] = F[j];
 }
 
 // Limited flux of the faces of one cell (res/Roe.cl:170-320), faces along [2, S-2]
-template <typename real, int D, int LIM = -1>
+template <typename real, int D, int LIM = -1, bool REC = false>
 __device__ __forceinline__ void roeFluxCell(const Grid& g, int lim, const StepConst<real>& sc,
                                             const real* __restrict__ stage, const real* __restrict__ basis,
                                             const real* __restrict__ dq, real* __restrict__ flux, long long c, int x,
-                                            int y, int z) {
+                                            int y, int z, real* __restrict__ tape = nullptr) {
     real sR[D + 2];
     loadState<real, D>(stage, c, sR);
-    if (roeFace(g, 0, x, y, z, 2, 1)) fluxFace<real, D, 0, LIM>(g, lim, sc.dt_dx[0], stage, basis, dq, flux, c, sR);
+    if (roeFace(g, 0, x, y, z, 2, 1))
+        fluxFace<real, D, 0, LIM, REC>(g, lim, sc.dt_dx[0], stage, basis, dq, flux, c, sR, tape);
     if (D > 1 && roeFace(g, 1, x, y, z, 2, 1))
-        fluxFace<real, D, (D > 1 ? 1 : 0), LIM>(g, lim, sc.dt_dx[1], stage, basis, dq, flux, c, sR);
+        fluxFace<real, D, (D > 1 ? 1 : 0), LIM, REC>(g, lim, sc.dt_dx[1], stage, basis, dq, flux, c, sR, tape);
     if (D > 2 && roeFace(g, 2, x, y, z, 2, 1))
-        fluxFace<real, D, (D > 2 ? 2 : 0), LIM>(g, lim, sc.dt_dx[2], stage, basis, dq, flux, c, sR);
+        fluxFace<real, D, (D > 2 ? 2 : 0), LIM, REC>(g, lim, sc.dt_dx[2], stage, basis, dq, flux, c, sR, tape);
 }
 
 }  // namespace hgpu
