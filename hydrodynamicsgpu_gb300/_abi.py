@@ -15,7 +15,7 @@ STATUS_NAMES = {
     8: "HGPU_ERR_NOMEM",
 }
 
-SOLVERS = {"EulerRoe": 0, "EulerHLLC": 1}
+SOLVERS = {"EulerRoe": 0, "EulerHLLC": 1, "EulerHLL": 2}
 BOUNDARIES = {"NONE": -1, "PERIODIC": 0, "MIRROR": 1, "FREEFLOW": 2}
 LIMITERS = ["DonorCell", "LaxWendroff", "BeamWarming", "Fromm", "CHARM", "HCUS", "HQUICK",
             "Koren", "MinMod", "Oshker", "Ospre", "Smart", "Sweby", "UMIST", "VanAlbada1",

@@ -39,7 +39,8 @@ BatchSolver<real>::BatchSolver(const std::vector<hgpu_config>& cfgs) {
     }
     dim_ = r0.dim;
     N_ = r0.numStates;
-    hllc_ = r0.cfg.solver == HGPU_SOLVER_HLLC;
+    hllc_ = r0.cfg.solver != HGPU_SOLVER_ROE;        // the HLL driver: EulerHLLC or EulerHLL
+    kind_ = r0.cfg.solver;
     integ_ = r0.cfg.integrator;
     cudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
     // offsets: each problem's cells start on a multiple of 32
@@ -159,7 +160,7 @@ void BatchSolver<real>::update() {                       // Solver::update for e
     L.boundary(nextQ());
     ++launches_;
     if (hllc_) {
-        L.waves(nextQ());                                 // HLL::initStep
+        L.waves(kind_ == HGPU_SOLVER_HLL, nextQ());       // HLL::initStep
         ++launches_;
     }
     if (!fixed) {
@@ -178,7 +179,8 @@ void BatchSolver<real>::update() {                       // Solver::update for e
             L.deltaQ(2, 1, in, dq_.as<real>(), nextQ());
             ++launches_;
         }
-        L.flux(hllc_, lim, sc, in, hllc_ ? nullptr : dq_.as<real>(), flux_.as<real>(), health, nextQ());
+        L.flux(kind_ == HGPU_SOLVER_ROE ? 0 : (kind_ == HGPU_SOLVER_HLL ? 2 : 1), lim, sc, in,
+               hllc_ ? nullptr : dq_.as<real>(), flux_.as<real>(), health, nextQ());
         L.combine(flux_.as<real>(), plan, sc, nextQ());
         launches_ += 2;
     };
@@ -293,7 +295,7 @@ std::string BatchSolver<real>::signature() const {
             h *= 1099511628211ULL;
         }
     std::ostringstream s;
-    s << (hllc_ ? "hllc" : "roe") << "-" << dim_ << "d-i" << integ_ << "-" << (sizeof(real) == 8 ? "f64" : "f32")
+    s << (kind_ == HGPU_SOLVER_ROE ? "roe" : kind_ == HGPU_SOLVER_HLL ? "hll" : "hllc") << "-" << dim_ << "d-i" << integ_ << "-" << (sizeof(real) == 8 ? "f64" : "f32")
       << "-p" << host_.size() << "-" << std::hex << h;
     return s.str();
 }

@@ -49,7 +49,7 @@ private:
     static constexpr int kQueues = 32;
     std::vector<ResolvedConfig> rcs_;
     std::vector<BatchProblem<real>> host_;
-    int dim_ = 0, N_ = 0, integ_ = 0, nTiles_ = 0, launches_ = 0;
+    int dim_ = 0, N_ = 0, integ_ = 0, nTiles_ = 0, launches_ = 0, kind_ = 0;
     bool hllc_ = false, alphaBinary_ = true;
     long long totalCells_ = 0;
     double tunedMs_ = 0;

@@ -80,7 +80,7 @@ ResolvedConfig resolveConfig(const hgpu_config& cfg) {
         if (i < dim && cfg.size[i] < 5) throw ConfigError(HGPU_ERR_CONFIG, "size must be >= 5 on every active axis");
         if (i >= dim && cfg.size[i] != 1) throw ConfigError(HGPU_ERR_CONFIG, "size must be 1 beyond dim");
     }
-    if (cfg.solver != HGPU_SOLVER_ROE && cfg.solver != HGPU_SOLVER_HLLC)
+    if (cfg.solver != HGPU_SOLVER_ROE && cfg.solver != HGPU_SOLVER_HLLC && cfg.solver != HGPU_SOLVER_HLL)
         throw ConfigError(HGPU_ERR_CONFIG, "unknown solver");
     if (cfg.limiter < 0 || cfg.limiter >= HGPU_NUM_LIMITERS) throw ConfigError(HGPU_ERR_CONFIG, "unknown slope limiter");
     if (cfg.integrator < 0 || cfg.integrator >= HGPU_NUM_INTEGRATORS)
@@ -308,7 +308,7 @@ unsigned long long Solver<real>::accInit() const {
     // Roe writes every dtBuffer entry (INFINITY outside the interior); HLLC writes only
     // the first volume entries, the rest keep their initial max() (Solver.cpp:217-222,
     // EulerHLLC.cl:135-168), which joins the minimum when dim > 1.
-    bool maxInit = rc.cfg.solver == HGPU_SOLVER_HLLC && rc.dim > 1;
+    bool maxInit = rc.cfg.solver != HGPU_SOLVER_ROE && rc.dim > 1;   // the HLL driver (HLLC and HLL)
     if (sizeof(real) == 8) {
         double v = maxInit ? DBL_MAX : std::numeric_limits<double>::infinity();
         unsigned long long b;
@@ -466,7 +466,7 @@ template <typename real>
 void HLL<real>::initStep() {                                 // HLL::initStep (HLL.cpp:31-33)
     this->launch("hllc_wave_speeds", 1, [&] {
         launchHllcWaves<real>(this->rc.grid, this->ph, this->state.template as<real>(), waves.template as<real>(),
-                              this->stream);
+                              this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream);
     });
 }
 
@@ -485,7 +485,8 @@ void HLL<real>::step() {                                     // HLL::step (HLL.c
         if (this->rc.cfg.compat == HGPU_COMPAT_SEAM && stage != this->state.template as<real>()) this->boundaryOn(stage);
         this->launch("hllc_flux", 1, [&] {
             launchHllcFlux<real>(this->rc.grid, this->ph, stage, waves.template as<real>(),
-                                 this->flux.template as<real>(), this->health, this->stream);
+                                 this->flux.template as<real>(), this->health, this->rc.cfg.solver == HGPU_SOLVER_HLL,
+                                 this->stream);
         });
     });
 }
@@ -500,6 +501,7 @@ template <typename real>
 static std::unique_ptr<SolverBase> makeSolver(const ResolvedConfig& rc) {
     std::unique_ptr<SolverBase> s;
     if (rc.cfg.solver == HGPU_SOLVER_ROE) s.reset(new EulerRoe<real>(rc));
+    else if (rc.cfg.solver == HGPU_SOLVER_HLL) s.reset(new EulerHLL<real>(rc));
     else s.reset(new EulerHLLC<real>(rc));
     s->init();
     return s;

@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) batchGravityKernel(const BatchProblem<rea
     }
 }
 
-template <typename real, int D>
+template <typename real, int D, bool HLL>
 __global__ void __launch_bounds__(256) batchWaveKernel(const BatchProblem<real>* __restrict__ P,
                                                        const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                        const real* __restrict__ state, real* __restrict__ waves,
@@ -179,7 +179,8 @@ __global__ void __launch_bounds__(256) batchWaveKernel(const BatchProblem<real>*
         long long c;
         if (!tileCell(pr.g, tl, tu, x, y, z, c)) continue;
         double gq = ((double)pr.ph.gamma + 1.) / (2. * (double)pr.ph.gamma);
-        hllcWaveCell<real, D>(pr.g, pr.ph, gq, state + (long long)(D + 2) * pr.stateOff, waves + pr.faceOff, c, x, y, z);
+        hllcWaveCell<real, D, HLL>(pr.g, pr.ph, gq, state + (long long)(D + 2) * pr.stateOff, waves + pr.faceOff, c, x,
+                                   y, z);
     }
 }
 
@@ -212,11 +213,17 @@ void BatchLaunch<real>::roeBasis(int loA, int hiA, unsigned* q) const {
 }
 
 template <typename real>
-void BatchLaunch<real>::waves(unsigned* q) const {
-#define L(DD) batchWaveKernel<real, DD><<<persistentBlocks(batchWaveKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, state, faces, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
+void BatchLaunch<real>::waves(int hll, unsigned* q) const {
+#define L(DD, H) batchWaveKernel<real, DD, H><<<persistentBlocks(batchWaveKernel<real, DD, H>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, state, faces, q)
+    if (hll) {
+        if (dim == 1) L(1, true);
+        else if (dim == 2) L(2, true);
+        else L(3, true);
+    } else {
+        if (dim == 1) L(1, false);
+        else if (dim == 2) L(2, false);
+        else L(3, false);
+    }
 #undef L
 }
 

@@ -44,11 +44,12 @@ struct BatchLaunch {
     real* faces;
     void boundary(unsigned* q) const;
     void roeBasis(int loA, int hiA, unsigned* q) const;
-    void waves(unsigned* q) const;
+    void waves(int hll, unsigned* q) const;
     void dt(int hllc, unsigned long long* acc, unsigned* health, unsigned* q) const;
     void finalize(int integ, unsigned long long* acc, StepConst<real>* sc) const;
     void deltaQ(int loA, int hiA, const real* stage, real* dq, unsigned* q) const;
-    void flux(int hllc, int lim, const StepConst<real>* sc, const real* stage, const real* dq, real* fluxBuf,
+    // kind: 0 EulerRoe, 1 EulerHLLC, 2 EulerHLL
+    void flux(int kind, int lim, const StepConst<real>* sc, const real* stage, const real* dq, real* fluxBuf,
               unsigned* health, unsigned* q) const;
     void combine(const real* fluxBuf, const CombinePlan<real>& plan, const StepConst<real>* sc, unsigned* q) const;
     void gravity(int integ, const StepConst<real>* sc, unsigned* q) const;

@@ -9,8 +9,9 @@
 namespace hgpu {
 namespace {
 
-// HLLC >= 0 and LIM >= 0 fix the solver and the slope limiter at compile time (the
-// kernel then carries one flux body and one limiter); -1 dispatches at run time
+// HLLC (0 EulerRoe, 1 EulerHLLC, 2 EulerHLL) and LIM >= 0 fix the solver and the
+// slope limiter at compile time (the kernel then carries one flux body and one
+// limiter); -1 dispatches at run time
 template <typename real, int D, int HLLC, int LIM>
 __global__ void __launch_bounds__(256) batchFluxKernel(const BatchProblem<real>* __restrict__ P,
                                                        const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
@@ -27,7 +28,10 @@ __global__ void __launch_bounds__(256) batchFluxKernel(const BatchProblem<real>*
         long long c;
         if (!tileCell(pr.g, tl, tu, x, y, z, c)) continue;
         const real* st = stage + (long long)(D + 2) * pr.stateOff;
-        if (HLLC == 1 || (HLLC < 0 && hllc)) {
+        if (HLLC == 2 || (HLLC < 0 && hllc == 2)) {
+            if (!hllcFluxCell<real, D, true>(pr.g, pr.ph, st, faces + pr.faceOff, flux + pr.dqOff, c, x, y, z))
+                atomicOr(health, HEALTH_HLLC_NOBRANCH);
+        } else if (HLLC == 1 || (HLLC < 0 && hllc == 1)) {
             if (!hllcFluxCell<real, D>(pr.g, pr.ph, st, faces + pr.faceOff, flux + pr.dqOff, c, x, y, z))
                 atomicOr(health, HEALTH_HLLC_NOBRANCH);
         } else {
@@ -55,7 +59,8 @@ static void batchFluxLaunch(const BatchLaunch<real>& b, int hllc, int lim, const
 template <typename real>
 void BatchLaunch<real>::flux(int hllc, int lim, const StepConst<real>* sc, const real* stage, const real* dq,
                              real* fluxBuf, unsigned* health, unsigned* q) const {
-    if (hllc) { batchFluxLaunch<real, 1, -1>(*this, hllc, lim, sc, stage, dq, fluxBuf, health, q); return; }
+    if (hllc == 1) { batchFluxLaunch<real, 1, -1>(*this, hllc, lim, sc, stage, dq, fluxBuf, health, q); return; }
+    if (hllc == 2) { batchFluxLaunch<real, 2, -1>(*this, hllc, lim, sc, stage, dq, fluxBuf, health, q); return; }
     switch (lim) {
     case HGPU_LIMITER_MINMOD: batchFluxLaunch<real, 0, HGPU_LIMITER_MINMOD>(*this, hllc, lim, sc, stage, dq, fluxBuf, health, q); break;
     case HGPU_LIMITER_SUPERBEE: batchFluxLaunch<real, 0, HGPU_LIMITER_SUPERBEE>(*this, hllc, lim, sc, stage, dq, fluxBuf, health, q); break;

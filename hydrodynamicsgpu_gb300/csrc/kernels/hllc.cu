@@ -8,6 +8,8 @@
 // limiter for HLLC is compiled out (:393-411), so the flux is first order.
 // A face where no HLLC branch applies keeps the flux of its previous evaluation,
 // momentum components swapped back once more, exactly as the reference buffer does.
+// With `hll` the same launches run EulerHLL (res/EulerHLL.cl): Davis-bounded wave
+// speeds and the two-state HLL flux; its timestep kernel is HLLC's.
 #include "hllc_cells.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
@@ -18,14 +20,14 @@ namespace {
 constexpr int kThreads = 256;
 inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
-template <typename real, int D>
+template <typename real, int D, bool HLL>
 __global__ void __launch_bounds__(kThreads) hllcWaveKernel(Grid g, Phys<real> ph, double gq,
                                                            const real* __restrict__ state, real* __restrict__ waves) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    hllcWaveCell<real, D>(g, ph, gq, state, waves, c, x, y, z);
+    hllcWaveCell<real, D, HLL>(g, ph, gq, state, waves, c, x, y, z);
 }
 
 template <typename real, int D>
@@ -43,7 +45,7 @@ __global__ void __launch_bounds__(kThreads) hllcDtKernel(Grid g, Phys<real> ph, 
     blockMinToGlobal(best, acc);
 }
 
-template <typename real, int D>
+template <typename real, int D, bool HLL>
 __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph, const real* __restrict__ stage,
                                                            const real* __restrict__ waves, real* __restrict__ flux,
                                                            unsigned* health) {
@@ -51,18 +53,26 @@ __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    if (!hllcFluxCell<real, D>(g, ph, stage, waves, flux, c, x, y, z)) atomicOr(health, HEALTH_HLLC_NOBRANCH);
+    if (!hllcFluxCell<real, D, HLL>(g, ph, stage, waves, flux, c, x, y, z)) atomicOr(health, HEALTH_HLLC_NOBRANCH);
 }
 
 }  // namespace
 
 template <typename real>
-void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, cudaStream_t st) {
+void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st) {
     // (gamma + 1.) / (2. * gamma) is a per-program constant (double literals); computed once, identically
     double gq = ((double)ph.gamma + 1.) / (2. * (double)ph.gamma);
-    if (g.dim == 1) hllcWaveKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
-    else if (g.dim == 2) hllcWaveKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
-    else hllcWaveKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves);
+#define L(DD, H) hllcWaveKernel<real, DD, H><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves)
+    if (hll) {
+        if (g.dim == 1) L(1, true);
+        else if (g.dim == 2) L(2, true);
+        else L(3, true);
+    } else {
+        if (g.dim == 1) L(1, false);
+        else if (g.dim == 2) L(2, false);
+        else L(3, false);
+    }
+#undef L
 }
 
 template <typename real>
@@ -75,18 +85,26 @@ void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsign
 
 template <typename real>
 void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                    unsigned* health, cudaStream_t st) {
-    if (g.dim == 1) hllcFluxKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health);
-    else if (g.dim == 2) hllcFluxKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health);
-    else hllcFluxKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health);
+                    unsigned* health, int hll, cudaStream_t st) {
+#define L(DD, H) hllcFluxKernel<real, DD, H><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health)
+    if (hll) {
+        if (g.dim == 1) L(1, true);
+        else if (g.dim == 2) L(2, true);
+        else L(3, true);
+    } else {
+        if (g.dim == 1) L(1, false);
+        else if (g.dim == 2) L(2, false);
+        else L(3, false);
+    }
+#undef L
 }
 
 #define INST(real)                                                                                                \
-    template void launchHllcWaves<real>(const Grid&, const Phys<real>&, const real*, real*, cudaStream_t);        \
+    template void launchHllcWaves<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t);   \
     template void launchHllcDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                      cudaStream_t);                                                               \
     template void launchHllcFlux<real>(const Grid&, const Phys<real>&, const real*, const real*, real*, unsigned*, \
-                                       cudaStream_t);
+                                       int, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

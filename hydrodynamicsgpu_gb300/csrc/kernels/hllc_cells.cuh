@@ -64,12 +64,49 @@ __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, do
     waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + mulI(cR, qR);
 }
 
+// EulerHLL sl, sr of one face (EulerHLL.cl:17-116): Davis direct bounded,
+// sl = min(vL - cL, v - c), sr = max(vR + cR, v + c) with v, c from the Roe averages.
+// `.5 * velocitySq` and `(gamma - 1.)` are double literals there (FP32 promotes).
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void hllWaveFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ state,
+                                            real* __restrict__ waves, long long c) {
+    real sL[D + 2], sR[D + 2];
+    loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
+    loadRotated<real, D, SIDE>(state, c, sR);
+    const double gm1 = (double)ph.gamma - 1.;
+    Prim<real, D> L, R;
+    primitives<real, D>(sL, ph.gamma, L);
+    primitives<real, D>(sR, ph.gamma, R);
+    const real cL = (real)sqrt(mulI(gm1, (double)L.enthalpyTotal - halfOf((double)L.velocitySq)));
+    const real cR = (real)sqrt(mulI(gm1, (double)R.enthalpyTotal - halfOf((double)R.velocitySq)));
+    const real wL = sqrt(L.density), wR = sqrt(R.density);
+    const real norm = (real)divI(1., (double)(wL + wR));
+    real v[3], vv;
+#pragma unroll
+    for (int k = 0; k < D; ++k) v[k] = mulI(mulI(wL, L.v[k]) + mulI(wR, R.v[k]), norm);
+    const real H = mulI(mulI(wL, L.enthalpyTotal) + mulI(wR, R.enthalpyTotal), norm);
+    vv = mulI(v[0], v[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) vv = vv + mulI(v[k], v[k]);
+    // (the Roe-averaged potential energy is +0: subtracting it changes no bit)
+    const real cs = (real)sqrt(mulI(gm1, (double)H - halfOf((double)vv)));
+    waves[((long long)SIDE * 2 + 0) * g.V + c] = fminLibm(L.v[0] - cL, v[0] - cs);
+    waves[((long long)SIDE * 2 + 1) * g.V + c] = fmaxLibm(R.v[0] + cR, v[0] + cs);
+}
+
 // wave speeds of the faces of one cell: every axis in [2, S-2] (EulerHLLC.cl:110-131)
-template <typename real, int D>
+// (HLL: EulerHLL's wave speeds instead, EulerHLL.cl:118-138)
+template <typename real, int D, bool HLL = false>
 __device__ __forceinline__ void hllcWaveCell(const Grid& g, const Phys<real>& ph, double gq,
                                              const real* __restrict__ state, real* __restrict__ waves, long long c,
                                              int x, int y, int z) {
     if (!inRange(g, x, y, z, 2, 1)) return;
+    if (HLL) {
+        hllWaveFace<real, D, 0>(g, ph, state, waves, c);
+        if (D > 1) hllWaveFace<real, D, (D > 1 ? 1 : 0)>(g, ph, state, waves, c);
+        if (D > 2) hllWaveFace<real, D, (D > 2 ? 2 : 0)>(g, ph, state, waves, c);
+        return;
+    }
     waveFace<real, D, 0>(g, ph, gq, state, waves, c);
     if (D > 1) waveFace<real, D, (D > 1 ? 1 : 0)>(g, ph, gq, state, waves, c);
     if (D > 2) waveFace<real, D, (D > 2 ? 2 : 0)>(g, ph, gq, state, waves, c);
@@ -163,9 +200,59 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
     return taken;
 }
 
+// EulerHLL flux (EulerHLL.cl:185-346): fL, fR, or the two-state HLL flux
+// (sr fL - sl fR + sl sr (uR - uL)) / (sr - sl); `flux` holds the face's previous value.
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
+                                        const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c) {
+    const int N = D + 2, E = N - 1;
+    real stL[N], stR[N];
+    loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
+    loadRotated<real, D, SIDE>(stage, c, stR);
+    Prim<real, D> L, R;
+    primitives<real, D>(stL, ph.gamma, L);
+    primitives<real, D>(stR, ph.gamma, R);
+    const real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
+    const real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
+    real fL[N], fR[N], flux[N];
+    fL[0] = mulI(L.density, L.v[0]);
+    fL[1] = mulI(mulI(L.density, L.v[0]), L.v[0]) + L.pressure;
+#pragma unroll
+    for (int k = 1; k < D; ++k) fL[1 + k] = mulI(mulI(L.density, L.v[k]), L.v[0]);
+    fL[E] = mulI(mulI(L.density, L.enthalpyTotal), L.v[0]);
+    fR[0] = mulI(R.density, R.v[0]);
+    fR[1] = mulI(mulI(R.density, R.v[0]), R.v[0]) + R.pressure;
+#pragma unroll
+    for (int k = 1; k < D; ++k) fR[1 + k] = mulI(mulI(R.density, R.v[k]), R.v[0]);
+    fR[E] = mulI(mulI(R.density, R.enthalpyTotal), R.v[0]);
+    bool taken = true;
+    if ((real)0. <= sl) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[i] = fL[i];
+    } else if (sl <= (real)0. && (real)0. <= sr) {
+        const real invDenom = (real)divI(1., (double)(sr - sl));
+        const real slsr = mulI(sl, sr);
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            flux[i] = mulI(mulI(sr, fL[i]) - mulI(sl, fR[i]) + mulI(slsr, stR[i] - stL[i]), invDenom);
+    } else if (sr <= (real)0.) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[i] = fR[i];
+    } else {
+        taken = false;                       // no branch: the previous (global-frame) value, swapped again
+#pragma unroll
+        for (int j = 0; j < N; ++j) flux[j] = fluxBuf[((long long)SIDE * N + j) * g.V + c];
+    }
+    if (SIDE > 0) { real t = flux[1]; flux[1] = flux[1 + SIDE]; flux[1 + SIDE] = t; }
+#pragma unroll
+    for (int j = 0; j < N; ++j) fluxBuf[((long long)SIDE * N + j) * g.V + c] = flux[j];
+    return taken;
+}
+
 // HLLC fluxes of the faces of one cell: along [2, S-2], transverse interior [2, S-3]
 // (the faces calcFluxDeriv reads).  Returns false if a face took no flux branch.
-template <typename real, int D>
+// (HLL: the EulerHLL flux instead)
+template <typename real, int D, bool HLL = false>
 __device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
                                              const real* __restrict__ waves, real* __restrict__ flux, long long c,
                                              int x, int y, int z) {
@@ -179,9 +266,15 @@ __device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph
             if (cc[a] < 2 || cc[a] >= g.S[a] - hi) in = false;
         }
         if (!in) continue;
-        if (side == 0) ok &= hllcFace<real, D, 0>(g, ph, stage, waves, flux, c);
-        else if (side == 1) ok &= hllcFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
-        else ok &= hllcFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+        if (HLL) {
+            if (side == 0) ok &= hllFace<real, D, 0>(g, ph, stage, waves, flux, c);
+            else if (side == 1) ok &= hllFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
+            else ok &= hllFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+        } else {
+            if (side == 0) ok &= hllcFace<real, D, 0>(g, ph, stage, waves, flux, c);
+            else if (side == 1) ok &= hllcFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
+            else ok &= hllcFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+        }
     }
     return ok;
 }

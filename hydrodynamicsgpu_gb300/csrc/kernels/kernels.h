@@ -66,13 +66,13 @@ int roeRecordSize(int dim);
 
 // ---- hllc.cu ----
 template <typename real>
-void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, cudaStream_t st);
+void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st);
 template <typename real>
 void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsigned long long* acc, unsigned* health,
                   cudaStream_t st);
 template <typename real>
 void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                    unsigned* health, cudaStream_t st);
+                    unsigned* health, int hll, cudaStream_t st);
 
 // ---- tableaus (combine.cu): alpha/beta in double, order ----
 int tableauOrder(int integrator);

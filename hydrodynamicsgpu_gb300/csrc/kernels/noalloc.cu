@@ -98,8 +98,51 @@ __device__ __forceinline__ void hllcSpeeds(const real* sL, const real* sR, real 
     sr = v0[1] + cc[1] * qR;
 }
 
+template <typename real, int D>
+__device__ __forceinline__ void hllSpeeds(const real* sL, const real* sR, real gamma, real& sl, real& sr) {
+    // EulerHLL.cl:54-113 in the rotated frame: Davis bounded with the Roe averages;
+    // `.5 * velocitySq` and `(gamma - 1.)` are double literals there
+    const int E = D + 1;
+    real rho[2] = {sL[0], sR[0]}, v[2][3], hT[2], cc[2], w[2];
+    const real* ss[2] = {sL, sR};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const real* x = ss[q];
+        real invDensity = (real)(1. / (double)rho[q]);
+#pragma unroll
+        for (int k = 0; k < D; ++k) v[q][k] = x[1 + k] / rho[q];
+        real vv = v[q][0] * v[q][0];
+#pragma unroll
+        for (int k = 1; k < D; ++k) vv = vv + v[q][k] * v[q][k];
+        real eT = x[E] * invDensity;
+        real eI = eT - (real)(.5 * (double)vv);
+        real p = (real)(((double)gamma - 1.) * (double)rho[q] * (double)eI);
+        hT[q] = eT + p * invDensity;
+        cc[q] = (real)sqrt(((double)gamma - 1.) * ((double)hT[q] - .5 * (double)vv));
+        w[q] = sqrt(rho[q]);
+    }
+    real norm = (real)(1. / (double)(w[0] + w[1]));
+    real vr[3], vvr;
+#pragma unroll
+    for (int k = 0; k < D; ++k) vr[k] = (w[0] * v[0][k] + w[1] * v[1][k]) * norm;
+    real H = (w[0] * hT[0] + w[1] * hT[1]) * norm;
+    vvr = vr[0] * vr[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) vvr = vvr + vr[k] * vr[k];
+    real cs = (real)sqrt(((double)gamma - 1.) * ((double)H - .5 * (double)vvr));
+    sl = fminLibm(v[0][0] - cc[0], vr[0] - cs);
+    sr = fmaxLibm(v[1][0] + cc[1], vr[0] + cs);
+}
+
+template <typename real, int D>
+__device__ __forceinline__ void familySpeeds(int hll, const real* sL, const real* sR, real gamma, double gq, real& sl,
+                                             real& sr) {
+    if (hll) hllSpeeds<real, D>(sL, sR, gamma, sl, sr);
+    else hllcSpeeds<real, D>(sL, sR, gamma, gq, sl, sr);
+}
+
 template <typename real, int D, int SIDE>
-__device__ __forceinline__ real hllcSideDt(const Grid& g, const Phys<real>& ph, double gq,
+__device__ __forceinline__ real hllcSideDt(const Grid& g, const Phys<real>& ph, double gq, int hll,
                                            const real* __restrict__ st, long long c, int coordAlong) {
     const int N = D + 2;
     const long long s = g.step[SIDE];
@@ -112,10 +155,10 @@ __device__ __forceinline__ real hllcSideDt(const Grid& g, const Phys<real>& ph, 
     real sl, sr, slNext = (real)0., srHere;
     load(c - s, a);
     load(c, b);
-    hllcSpeeds<real, D>(a, b, ph.gamma, gq, sl, srHere);
+    familySpeeds<real, D>(hll, a, b, ph.gamma, gq, sl, srHere);
     if (coordAlong + 1 <= g.S[SIDE] - 2) {        // face c+1 is computed only up to S-2
         load(c + s, a);
-        hllcSpeeds<real, D>(b, a, ph.gamma, gq, slNext, sr);
+        familySpeeds<real, D>(hll, b, a, ph.gamma, gq, slNext, sr);
     }
     real minLambda = (real)fmin(0., (double)slNext);
     real maxLambda = (real)fmax(0., (double)srHere);
@@ -153,16 +196,16 @@ __global__ void __launch_bounds__(kThreads) cflNoAllocKernel(Grid g, Phys<real> 
             }
         } else {
             if (inRange(g, xyz[0], xyz[1], xyz[2], 2, 1)) {
-                real d = hllcSideDt<real, D, 0>(g, ph, gq, st, c, xyz[0]);
+                real d = hllcSideDt<real, D, 0>(g, ph, gq, hllc == 2, st, c, xyz[0]);
                 nan |= d != d;
                 r = fmin(r, d);
                 if (D > 1) {
-                    d = hllcSideDt<real, D, (D > 1 ? 1 : 0)>(g, ph, gq, st, c, xyz[1]);
+                    d = hllcSideDt<real, D, (D > 1 ? 1 : 0)>(g, ph, gq, hllc == 2, st, c, xyz[1]);
                     nan |= d != d;
                     r = fmin(r, d);
                 }
                 if (D > 2) {
-                    d = hllcSideDt<real, D, (D > 2 ? 2 : 0)>(g, ph, gq, st, c, xyz[2]);
+                    d = hllcSideDt<real, D, (D > 2 ? 2 : 0)>(g, ph, gq, hllc == 2, st, c, xyz[2]);
                     nan |= d != d;
                     r = fmin(r, d);
                 }
@@ -210,7 +253,7 @@ __global__ void __launch_bounds__(kThreads) cflNoAllocKernel(Grid g, Phys<real> 
 template <typename real>
 unsigned long long initBits(int solver, int dim) {
     // Roe writes every dtBuffer entry; HLLC leaves entries V..V*dim-1 at max() (Solver.cpp:217-222)
-    bool maxInit = solver == HGPU_SOLVER_HLLC && dim > 1;
+    bool maxInit = solver != HGPU_SOLVER_ROE && dim > 1;
     real v = maxInit ? (sizeof(real) == 8 ? (real)DBL_MAX : (real)FLT_MAX) : (real)INFINITY;
     unsigned long long b = 0;
     memcpy(&b, &v, sizeof(real));
@@ -293,7 +336,7 @@ extern "C" int hgpu_cfl_timestep_noalloc(const hgpu_config* cfg, const void* d_s
         setLastError(std::string("scratch clear failed: ") + cudaGetErrorString(e));
         return HGPU_ERR_CUDA;
     }
-    int hllc = rc.cfg.solver == HGPU_SOLVER_HLLC;
+    int hllc = rc.cfg.solver == HGPU_SOLVER_ROE ? 0 : (rc.cfg.solver == HGPU_SOLVER_HLL ? 2 : 1);   // 2: EulerHLL
     if (rc.cfg.precision == HGPU_FP32) launchCfl<float>(rc, hllc, d_state, blocks, st);
     else launchCfl<double>(rc, hllc, d_state, blocks, st);
     unsigned long long bits = 0, flags = 0;

@@ -49,7 +49,8 @@ typedef enum hgpu_status {
 /* ---- solver family (src/HydroGPUApp.cpp:90-118 solver registry) ---- */
 enum {
     HGPU_SOLVER_ROE = 0,   /* "EulerRoe"  (src/Solver/EulerRoe.cpp)  */
-    HGPU_SOLVER_HLLC = 1   /* "EulerHLLC" (src/Solver/EulerHLLC.cpp) */
+    HGPU_SOLVER_HLLC = 1,  /* "EulerHLLC" (src/Solver/EulerHLLC.cpp) */
+    HGPU_SOLVER_HLL = 2    /* "EulerHLL"  (src/Solver/EulerHLL.cpp, res/EulerHLL.cl) */
 };
 
 /* ---- boundary methods (include/HydroGPU/Boundary/Boundary.h:8-14; the

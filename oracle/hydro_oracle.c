@@ -1,5 +1,5 @@
 /*
- * hydro_oracle.c -- CPU parity oracle for the HydroGPU Euler Roe/HLLC step.
+ * hydro_oracle.c -- CPU parity oracle for the HydroGPU Euler Roe/HLLC/HLL step.
  *
  * TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
  * CPU-baseline leg of bench.py as the checker; never linked into the product.
@@ -67,7 +67,8 @@ int oracle_resolve(const hgpu_config* cfg, int* dim_out, double dx[3], double* g
         if (i < dim && cfg->size[i] < 5) return HGPU_ERR_CONFIG;
         if (i >= dim && cfg->size[i] != 1) return HGPU_ERR_CONFIG;
     }
-    if (cfg->solver != HGPU_SOLVER_ROE && cfg->solver != HGPU_SOLVER_HLLC) return HGPU_ERR_CONFIG;
+    if (cfg->solver != HGPU_SOLVER_ROE && cfg->solver != HGPU_SOLVER_HLLC && cfg->solver != HGPU_SOLVER_HLL)
+        return HGPU_ERR_CONFIG;
     if (cfg->limiter < 0 || cfg->limiter >= HGPU_NUM_LIMITERS) return HGPU_ERR_CONFIG;
     if (cfg->integrator < 0 || cfg->integrator >= HGPU_NUM_INTEGRATORS) return HGPU_ERR_CONFIG;
     for (int i = 0; i < 3; ++i) {

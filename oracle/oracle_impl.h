@@ -36,7 +36,8 @@ typedef struct {
     REAL dx[3];        /* DX/DY/DZ as baked into the program (Solver.cpp:272-274) */
     REAL gamma;        /* ((real)<defs value>) (Solver.cpp:298)                  */
     float cfl;
-    int isHLLC;
+    int isHLLC;        /* an HLL-family solver (EulerHLLC or EulerHLL): HLL.cpp driver */
+    int isHLL;         /* EulerHLL: Davis-bounded wave speeds, two-state HLL flux     */
     REAL* state;       /* Solver::stateBuffer                                     */
     REAL* potential;   /* SelfGravitation::potentialBuffer (zero: useGravity=false) */
     REAL* eigenvalues; /* Roe: V*dim*N; HLL: V*dim*N                               */
@@ -537,6 +538,127 @@ static void FN(hllcFlux)(FN(osolver) * s) {
     }
 }
 
+/* ---------------- EulerHLL calcEigenvalues (EulerHLL.cl:17-138) ----------------
+ * Davis direct bounded wave speeds: sl = min(vL - cL, v - c), sr = max(vR + cR, v + c)
+ * with v, c from the Roe averages.  `.5 * velocitySq` and `(gamma - 1.)` are double
+ * literals here (EulerHLLC.cl writes `.5f`): FP32 evaluates them in double. */
+static void FN(hllEigenvalues)(FN(osolver) * s) {
+    const int N = s->N, E = N - 1, D = s->dim;
+    const REAL g = s->gamma;
+    FOR_CELLS(s) {
+        if (!FN(inRange)(s, x, y, z, 2, 1)) continue;
+        long index = IDX(s, x, y, z);
+        for (int side = 0; side < D; ++side) {
+            long indexPrev = index - s->step[side];
+            REAL sL[5], sR[5];
+            for (int i = 0; i < N; ++i) { sL[i] = s->state[i + N * indexPrev]; sR[i] = s->state[i + N * index]; }
+            { REAL t = sL[1]; sL[1] = sL[1 + side]; sL[1 + side] = t; t = sR[1]; sR[1] = sR[1 + side]; sR[1 + side] = t; }
+            REAL* lam = s->eigenvalues + N * (side + D * index);
+            REAL rhoL = sL[0];
+            REAL invDensityL = 1. / rhoL;
+            REAL vL[4], vR[4];
+            for (int k = 0; k < 4; ++k) vL[k] = (k < D ? sL[1 + k] : (REAL)0.f) / rhoL;
+            REAL velocitySqL = DOT4(vL, vL);
+            REAL energyTotalL = sL[E] * invDensityL;
+            REAL energyKineticL = .5 * velocitySqL;
+            REAL energyPotentialL = s->potential[indexPrev];
+            REAL energyInternalL = energyTotalL - energyKineticL - energyPotentialL;
+            REAL pressureL = (g - 1.) * rhoL * energyInternalL;
+            REAL enthalpyTotalL = energyTotalL + pressureL * invDensityL;
+            REAL speedOfSoundL = sqrt((g - 1.) * (enthalpyTotalL - .5 * velocitySqL));
+            REAL roeWeightL = sqrt(rhoL);
+            REAL rhoR = sR[0];
+            REAL invDensityR = 1. / rhoR;
+            for (int k = 0; k < 4; ++k) vR[k] = (k < D ? sR[1 + k] : (REAL)0.f) / rhoR;
+            REAL velocitySqR = DOT4(vR, vR);
+            REAL energyTotalR = sR[E] * invDensityR;
+            REAL energyKineticR = .5 * velocitySqR;
+            REAL energyPotentialR = s->potential[index];
+            REAL energyInternalR = energyTotalR - energyKineticR - energyPotentialR;
+            REAL pressureR = (g - 1.) * rhoR * energyInternalR;
+            REAL enthalpyTotalR = energyTotalR + pressureR * invDensityR;
+            REAL speedOfSoundR = sqrt((g - 1.) * (enthalpyTotalR - .5 * velocitySqR));
+            REAL roeWeightR = sqrt(rhoR);
+            REAL norm = 1. / (roeWeightL + roeWeightR);
+            REAL v[4];
+            for (int k = 0; k < 4; ++k) v[k] = (roeWeightL * vL[k] + roeWeightR * vR[k]) * norm;
+            REAL enthalpyTotal = (roeWeightL * enthalpyTotalL + roeWeightR * enthalpyTotalR) * norm;
+            REAL energyPotential = (roeWeightL * energyPotentialL + roeWeightR * energyPotentialR) * norm;
+            REAL velocitySq = DOT4(v, v);
+            REAL speedOfSound = sqrt((g - 1.) * (enthalpyTotal - .5 * velocitySq - energyPotential));
+            REAL eigenvaluesMinL = vL[0] - speedOfSoundL;
+            REAL eigenvaluesMaxR = vR[0] + speedOfSoundR;
+            REAL eigenvaluesMin = v[0] - speedOfSound;
+            REAL eigenvaluesMax = v[0] + speedOfSound;
+            lam[0] = (REAL)fmin(eigenvaluesMinL, eigenvaluesMin);
+            for (int k = 1; k < E; ++k) lam[k] = v[0];
+            lam[E] = (REAL)fmax(eigenvaluesMaxR, eigenvaluesMax);
+        }
+    }
+}
+
+/* ---------------- EulerHLL calcFlux (EulerHLL.cl:185-346): the two-state HLL flux ---------------- */
+static void FN(hllFlux)(FN(osolver) * s) {
+    const int N = s->N, E = N - 1, D = s->dim;
+    const REAL g = s->gamma;
+    FOR_CELLS(s) {
+        if (!FN(inRange)(s, x, y, z, 2, 1)) continue;
+        long index = IDX(s, x, y, z);
+        for (int side = 0; side < D; ++side) {
+            long indexPrev = index - s->step[side];
+            long iF = side + D * index;
+            REAL sL[5], sR[5];
+            for (int i = 0; i < N; ++i) { sL[i] = s->state[i + N * indexPrev]; sR[i] = s->state[i + N * index]; }
+            { REAL t = sL[1]; sL[1] = sL[1 + side]; sL[1 + side] = t; t = sR[1]; sR[1] = sR[1 + side]; sR[1 + side] = t; }
+            const REAL* lam = s->eigenvalues + N * iF;
+            REAL* flux = s->flux + N * iF;
+            REAL rhoL = sL[0];
+            REAL invDensityL = 1. / rhoL;
+            REAL vL[4], vR[4];
+            for (int k = 0; k < 4; ++k) vL[k] = (k < D ? sL[1 + k] : (REAL)0.f) / rhoL;
+            REAL velocitySqL = DOT4(vL, vL);
+            REAL energyTotalL = sL[E] * invDensityL;
+            REAL energyKineticL = .5 * velocitySqL;
+            REAL energyPotentialL = s->potential[indexPrev];
+            REAL energyInternalL = energyTotalL - energyKineticL - energyPotentialL;
+            REAL pressureL = (g - 1.) * rhoL * energyInternalL;
+            REAL enthalpyTotalL = energyTotalL + pressureL * invDensityL;
+            REAL rhoR = sR[0];
+            REAL invDensityR = 1. / rhoR;
+            for (int k = 0; k < 4; ++k) vR[k] = (k < D ? sR[1 + k] : (REAL)0.f) / rhoR;
+            REAL velocitySqR = DOT4(vR, vR);
+            REAL energyTotalR = sR[E] * invDensityR;
+            REAL energyKineticR = .5 * velocitySqR;
+            REAL energyPotentialR = s->potential[index];
+            REAL energyInternalR = energyTotalR - energyKineticR - energyPotentialR;
+            REAL pressureR = (g - 1.) * rhoR * energyInternalR;
+            REAL enthalpyTotalR = energyTotalR + pressureR * invDensityR;
+            REAL sl = lam[0], sr = lam[N - 1];
+            REAL fL[5], fR[5];
+            fL[0] = rhoL * vL[0];
+            fL[1] = rhoL * vL[0] * vL[0] + pressureL;
+            if (D > 1) fL[2] = rhoL * vL[1] * vL[0];
+            if (D > 2) fL[3] = rhoL * vL[2] * vL[0];
+            fL[E] = rhoL * enthalpyTotalL * vL[0];
+            fR[0] = rhoR * vR[0];
+            fR[1] = rhoR * vR[0] * vR[0] + pressureR;
+            if (D > 1) fR[2] = rhoR * vR[1] * vR[0];
+            if (D > 2) fR[3] = rhoR * vR[2] * vR[0];
+            fR[E] = rhoR * enthalpyTotalR * vR[0];
+            if (0. <= sl) {
+                for (int i = 0; i < N; ++i) flux[i] = fL[i];
+            } else if (sl <= 0. && 0. <= sr) {
+                REAL invDenom = 1. / (sr - sl);
+                for (int i = 0; i < N; ++i) flux[i] = (sr * fL[i] - sl * fR[i] + sl * sr * (sR[i] - sL[i])) * invDenom;
+            } else if (sr <= 0.) {
+                for (int i = 0; i < N; ++i) flux[i] = fR[i];
+            }
+            /* no branch taken: the buffer keeps its previous flux (stale), and is still rotated back */
+            { REAL t = flux[1]; flux[1] = flux[1 + side]; flux[1 + side] = t; }
+        }
+    }
+}
+
 /* ---------------- calcFluxDeriv (CalcFluxDeriv.cl:7-44) ---------------- */
 static void FN(calcFluxDeriv)(FN(osolver) * s, REAL* deriv) {
     const int N = s->N, D = s->dim;
@@ -589,7 +711,8 @@ static void FN(callback)(FN(osolver) * s, int kind, REAL* deriv, REAL dt) {
             FN(calcDeltaQTilde)(s);
             FN(roeFlux)(s, dt);
         } else {                       /* HLL::step callback (HLL.cpp:40-47) */
-            FN(hllcFlux)(s);
+            if (s->isHLL) FN(hllFlux)(s);
+            else FN(hllcFlux)(s);
         }
         FN(calcFluxDeriv)(s, deriv);
     } else {                           /* SelfGravitation::applyPotential (SelfGravitation.cpp:100-124) */
@@ -646,7 +769,10 @@ static REAL FN(findMinTimestep)(FN(osolver) * s, int* nonfinite) {
 
 static int FN(update)(FN(osolver) * s, int* nonfinite) {   /* Solver::update (Solver.cpp:521-546) */
     FN(boundary)(s);
-    if (s->isHLLC) FN(hllcEigenvalues)(s);                  /* HLL::initStep (HLL.cpp:31-33) */
+    if (s->isHLLC) {                                         /* HLL::initStep (HLL.cpp:31-33) */
+        if (s->isHLL) FN(hllEigenvalues)(s);
+        else FN(hllcEigenvalues)(s);
+    }
     REAL dt;
     if (s->cfg.use_fixed_dt) dt = (REAL)s->cfg.fixed_dt;
     else if (!s->isHLLC) {                                   /* Roe::calcTimestep (Roe.cpp:88-92) */
@@ -682,7 +808,8 @@ static FN(osolver) * FN(create)(const hgpu_config* cfg, int dim, const double dx
     s->V = (long)s->S[0] * s->S[1] * s->S[2];
     s->gamma = (REAL)gammaBaked;
     s->cfl = cfg->cfl;
-    s->isHLLC = cfg->solver == HGPU_SOLVER_HLLC;
+    s->isHLLC = cfg->solver == HGPU_SOLVER_HLLC || cfg->solver == HGPU_SOLVER_HLL;
+    s->isHLL = cfg->solver == HGPU_SOLVER_HLL;
     size_t vn = (size_t)s->V * s->N;
     s->state = (REAL*)calloc(vn, sizeof(REAL));
     s->potential = (REAL*)calloc((size_t)s->V, sizeof(REAL));

@@ -156,7 +156,7 @@ def refcl_available(cfg=None):
 def _refcl_path(cfg):
     dim = _abi.config_dim(cfg)
     return os.path.join(REF_DIR, "librefcl_%s_%dd_%s.so" % (
-        "roe" if cfg.solver == 0 else "hllc", dim, "f32" if cfg.precision == _abi.FP32 else "f64"))
+        ("roe", "hllc", "hll")[cfg.solver], dim, "f32" if cfg.precision == _abi.FP32 else "f64"))
 
 
 _refcl_libs = {}

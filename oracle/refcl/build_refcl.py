@@ -40,12 +40,12 @@ OUT = os.path.join(REPO, "oracle", "_ref")
 GEN = os.path.join(OUT, "gen")
 
 KERNEL_FILES = ["SlopeLimiter", "Common", "CalcFluxDeriv", "RoeEigenfieldLinear", "Roe",
-                "EulerRoe", "EulerHLLC", "SelfGravitation"]
+                "EulerRoe", "EulerHLLC", "EulerHLL", "SelfGravitation"]
 HEADER_FILES = ["Roe.h", "Euler.h"]
 LIMITERS = ["DonorCell", "LaxWendroff", "BeamWarming", "Fromm", "CHARM", "HCUS", "HQUICK",
             "Koren", "MinMod", "Oshker", "Ospre", "Smart", "Sweby", "UMIST", "VanAlbada1",
             "VanAlbada2", "VanLeer", "MonotizedCentral", "Superbee", "BarthJespersen"]
-VARIANTS = [(solver, dim, prec) for solver in ("roe", "hllc") for dim in (1, 2, 3) for prec in ("f64", "f32")]
+VARIANTS = [(solver, dim, prec) for solver in ("roe", "hllc", "hll") for dim in (1, 2, 3) for prec in ("f64", "f32")]
 
 
 def rewrite(text, const_inits):
@@ -137,8 +137,10 @@ def program_source(solver, dim, prec, const_inits):
         lines += ["#define EIGEN_TRANSFORM_STRUCT_SIZE %d" % (2 * n * n), "#define EIGEN_SPACE_DIM %d" % n,
                   '#include "RoeEigenfieldLinear.cl.inc"', '#include "Roe.cl.inc"',
                   '#include "SelfGravitation.cl.inc"', '#include "EulerRoe.cl.inc"']
-    else:
+    elif solver == "hllc":
         lines += ['#include "EulerHLLC.cl.inc"', '#include "SelfGravitation.cl.inc"']
+    else:
+        lines += ['#include "EulerHLL.cl.inc"', '#include "SelfGravitation.cl.inc"']
     names = sorted(set(const_inits))
     lines.append("static void refcl_init_constants() { %s }" % " ".join("refcl_init_%s();" % c for c in names))
     lines.append('#include "refcl_driver.inc"')

@@ -56,6 +56,14 @@ CASES = [
          cfg=dict(solver="EulerHLLC", size=(12, 12, 12), xmin=(0, 0, 0), xmax=(1, 1, 1), gamma=5. / 3.,
                   boundary="MIRROR", limiter="VanLeer", integrator="RungeKutta2TVD", cfl=.4),
          init=lambda: ic.lognormal_grf(size=(12, 12, 12), corr_cells=3.0, seed=1)),
+    dict(name="quad3_hll_rk2heun_freeflow_2d", steps=5,
+         cfg=dict(solver="EulerHLL", size=(24, 24), boundary="FREEFLOW", limiter="MinMod",
+                  integrator="RungeKutta2Heun", cfl=.5),
+         init=lambda: ic.configuration(3, size=(24, 24))),
+    dict(name="sod_hll_rk4_mirror_1d", steps=10,
+         cfg=dict(solver="EulerHLL", size=(64,), xmin=(0.,), xmax=(1.,), boundary="MIRROR", limiter="MinMod",
+                  integrator="RungeKutta4", cfl=.5),
+         init=lambda: ic.sod(size=(64,))),
     dict(name="roe_rk3tvd_umist_mirror_3d", steps=3,
          cfg=dict(solver="EulerRoe", size=(10, 9, 8), boundary="MIRROR", limiter="UMIST",
                   integrator="RungeKutta3TVD", cfl=.4),

@@ -84,6 +84,12 @@ def test_hllc_batch_matches_alone(hg, dim, integrator):
     check_batch(hg, mixed_configs("EulerHLLC", dim, integrator, "Superbee", n=6, seed=10 + dim), blocky=False)
 
 
+@pytest.mark.parametrize("integrator", ["ForwardEuler", "RungeKutta2", "RungeKutta4"])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_hll_batch_matches_alone(hg, dim, integrator):
+    check_batch(hg, mixed_configs("EulerHLL", dim, integrator, "Superbee", n=6, seed=50 + dim), blocky=False)
+
+
 @pytest.mark.parametrize("limiter", ["MinMod", "VanLeer", "MonotizedCentral", "DonorCell", "LaxWendroff"])
 def test_roe_batch_limiters(hg, limiter):
     check_batch(hg, mixed_configs("EulerRoe", 2, "RungeKutta2", limiter, n=4, seed=3), steps=2, blocky=False)

@@ -184,3 +184,28 @@ def test_step_aliases_match_update(hg):
     assert same(ba.get_state(1), bb.get_state(1))
     for x in (a, b, ba, bb):
         x.close()
+
+
+@pytest.mark.parametrize("dim,bnd", list(itertools.product([1, 2, 3], BOUNDARIES)))
+@pytest.mark.parametrize("integrator", ["ForwardEuler", "RungeKutta2", "RungeKutta4", "RungeKutta3TVD",
+                                        "RungeKutta4TVD"])
+def test_hll_integrators_boundaries(hg, oracle_mod, dim, bnd, integrator):
+    """EulerHLL (res/EulerHLL.cl): Davis-bounded wave speeds, two-state HLL flux."""
+    cfg = _abi.make_config(solver="EulerHLL", size=SMALL[dim], boundary=bnd, integrator=integrator)
+    run_pair(hg, oracle_mod, cfg, random_state(cfg, seed=20 + dim, blocky=True), steps=3)
+
+
+def test_hll_kh_and_quadrants(hg, oracle_mod):
+    cfg = _abi.make_config(solver="EulerHLL", size=(64, 64), boundary="PERIODIC", integrator="RungeKutta4")
+    run_pair(hg, oracle_mod, cfg, ic.kelvin_helmholtz(size=(64, 64), seed=2).reshape(-1), steps=10)
+    for n in (1, 3, 6):
+        cfg = _abi.make_config(solver="EulerHLL", size=(32, 32), boundary="FREEFLOW", integrator="RungeKutta2",
+                               cfl=.475)
+        run_pair(hg, oracle_mod, cfg, ic.configuration(n, size=(32, 32)).reshape(-1), steps=6)
+
+
+def test_hll_fp32(hg, oracle_mod):
+    cfg = _abi.make_config(solver="EulerHLL", size=(48, 40), boundary="PERIODIC", integrator="RungeKutta2",
+                           precision=_abi.FP32)
+    err, dterr = run_pair(hg, oracle_mod, cfg, random_state(cfg, seed=4), steps=100, exact=False)
+    assert err <= FP32_TOL and dterr <= FP32_TOL, (err, dterr)

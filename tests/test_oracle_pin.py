@@ -38,7 +38,7 @@ def pin(mod, cfg, init, steps):
 
 CASES = []
 for solver, dim, integ, bnd, prec in itertools.product(
-        ["EulerRoe", "EulerHLLC"], [1, 2, 3], _abi.INTEGRATORS, ["PERIODIC", "MIRROR", "FREEFLOW"], [0, 1]):
+        ["EulerRoe", "EulerHLLC", "EulerHLL"], [1, 2, 3], _abi.INTEGRATORS, ["PERIODIC", "MIRROR", "FREEFLOW"], [0, 1]):
     CASES.append((solver, dim, integ, bnd, prec))
 
 
@@ -57,7 +57,7 @@ def test_pin_limiters(refcl, limiter, blocky):
     pin(refcl, cfg, random_state(cfg, seed=3, blocky=blocky), steps=1 if blocky else 3)
 
 
-@pytest.mark.parametrize("solver", ["EulerRoe", "EulerHLLC"])
+@pytest.mark.parametrize("solver", ["EulerRoe", "EulerHLLC", "EulerHLL"])
 def test_pin_fixed_dt(refcl, solver):
     cfg = _abi.make_config(solver=solver, size=SMALL[2], boundary="FREEFLOW", integrator="RungeKutta4",
                            use_fixed_dt=True, fixed_dt=2e-3)

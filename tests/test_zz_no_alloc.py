@@ -21,7 +21,8 @@ from hydrodynamicsgpu_gb300 import initconds as ic
 pytestmark = pytest.mark.gpu
 
 CASES = [("EulerRoe", _abi.FP64, (96, 80)), ("EulerHLLC", _abi.FP64, (96, 80)),
-         ("EulerRoe", _abi.FP32, (64, 72)), ("EulerHLLC", _abi.FP64, (24, 20, 18))]
+         ("EulerRoe", _abi.FP32, (64, 72)), ("EulerHLLC", _abi.FP64, (24, 20, 18)),
+         ("EulerHLL", _abi.FP64, (96, 80)), ("EulerHLL", _abi.FP32, (30, 26, 22))]
 
 
 @pytest.mark.parametrize("solver,precision,size", CASES)
