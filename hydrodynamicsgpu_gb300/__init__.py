@@ -57,6 +57,9 @@ SIGNATURES = {
     "hgpu_checkpoint_destroy": (ctypes.c_int, [_P]),
     "hgpu_fp64_selftest": (ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_longlong)]),
+    "hgpu_display": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t]),
+    "hgpu_display_device": (ctypes.c_int, [_P, ctypes.c_int, _P]),
+    "hgpu_save_fits": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]),
     "hgpu_batch_create": (ctypes.c_int, [_CFG, ctypes.c_int, ctypes.POINTER(_P)]),
     "hgpu_batch_destroy": (ctypes.c_int, [_P]),
     "hgpu_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
@@ -275,19 +278,21 @@ class Solver:
         check(lib().hgpu_adjoint_step(self.h, ctypes.c_void_p(d_u), ctypes.c_void_p(d_lam_next),
                                       ctypes.c_void_p(d_lam_out), float(dt)))
 
-    def save(self, prefix):
-        """Solver::save (src/Solver/Solver.cpp:563-589) without the FITS dependency:
-        one little-endian raw file per state channel, <prefix><STATE>.raw, plus
-        <prefix>header.json describing sizes and dtype."""
-        import json
-        names = ["DENSITY", "MOMENTUM_X", "MOMENTUM_Y", "MOMENTUM_Z"][: 1 + self.dim] + ["ENERGY_TOTAL"]
-        st = self.getState().reshape(self.shape())
-        for j, n in enumerate(names):
-            np.ascontiguousarray(st[..., j]).astype("<" + np.dtype(self.dtype).str[1:]).tofile(prefix + n + ".raw")
-        with open(prefix + "header.json", "w") as f:
-            json.dump({"size": list(self.cfg.size), "dtype": np.dtype(self.dtype).name, "channels": names,
-                       "frame": self.frame}, f)
-        return names
+    def save(self, directory="."):
+        """Solver::save (src/Solver/Solver.cpp:549-589): <CHANNEL><index>.fits per state
+        channel plus `potential`, 32-bit float images; returns the save index."""
+        idx = ctypes.c_int()
+        check(lib().hgpu_save_fits(self.h, str(directory).encode(), ctypes.byref(idx)))
+        return idx.value
+
+    def display(self, method):
+        """convertToTex (res/EulerMHDCommon.cl:4-116): the display scalar of every cell
+        as float32, shaped like the grid; `method` is a name of DISPLAY_NAMES(dim) or
+        the reference's DISPLAY_* index."""
+        m = _abi.display_index(self.dim, method)
+        out = np.empty(self.count // self.num_states, dtype=np.float32)
+        check(lib().hgpu_display(self.h, m, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), out.size))
+        return out.reshape(self.shape()[:-1])
 
 
 class BatchTuning(ctypes.Structure):

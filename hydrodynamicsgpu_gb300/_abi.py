@@ -113,3 +113,19 @@ def config_volume(cfg):
 
 def config_count(cfg):
     return config_volume(cfg) * (config_dim(cfg) + 2)
+
+
+def display_names(dim):
+    """The reference's DISPLAY_* enum for Euler in `dim` dimensions (Euler.cpp:18-27)."""
+    return (["DENSITY", "VELOCITY", "VELOCITY_X"] + (["VELOCITY_Y"] if dim > 1 else []) +
+            (["VELOCITY_Z"] if dim > 2 else []) +
+            ["PRESSURE", "ENERGY_INTERNAL", "ENERGY_KINETIC", "ENERGY_TOTAL", "POTENTIAL"])
+
+
+def display_index(dim, method):
+    if isinstance(method, str):
+        names = display_names(dim)
+        if method.upper() not in names:
+            raise ValueError("unknown display method %r for dim %d" % (method, dim))
+        return names.index(method.upper())
+    return int(method)

@@ -29,6 +29,8 @@ SOURCES = {
     "kernels/batch_flux.cu": ["--fmad=false"],
     "kernels/adjoint.cu": [],
     "kernels/roe_record.cu": ["--fmad=false"],
+    "kernels/display.cu": ["--fmad=false"],
+    "host/fits.cu": [],
     "host/adjoint.cu": [],
     "host/batch_solver.cu": [],
     "host/solver.cu": [],
@@ -37,7 +39,7 @@ SOURCES = {
 HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
            "kernels/combine_cells.cuh", "kernels/batch.h", "kernels/batch_common.cuh", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",
            "kernels/adjoint.h", "host/adjoint.h",
-           "kernels/limiter_dual.cuh"]
+           "kernels/limiter_dual.cuh", "host/fits.h"]
 
 
 def nvcc():

@@ -8,6 +8,7 @@
 
 #include "adjoint.h"
 #include "batch_solver.h"
+#include "fits.h"
 #include "solver.h"
 
 namespace hgpu {
@@ -25,6 +26,7 @@ struct hgpu_solver {
     int kernelsPerStep = 0;
     std::unique_ptr<hgpu::RoeAdjoint> adjoint;   // created on first use
     std::vector<hgpu_checkpoint*> checkpoints;   // live trajectories of this solver
+    hgpu::DeviceBuffer display;                   // one float per cell, created on first use
 };
 
 struct hgpu_checkpoint {
@@ -493,6 +495,82 @@ int hgpu_batch_autotune(hgpu_batch* b, const char* cache_path, int steps) {
     if (!b || steps <= 0) return fail(HGPU_ERR_ARG, "bad argument");
     return guarded([&]() {
         b->b->autotune(cache_path ? std::string(cache_path) : std::string(), steps);
+        return (int)HGPU_OK;
+    });
+}
+
+extern "C++" {
+namespace {
+template <typename real>
+bool displayAs(hgpu::SolverBase* b, int method, float* d_out) {
+    auto* s = dynamic_cast<hgpu::Solver<real>*>(b);
+    if (!s) return false;
+    hgpu::launchDisplay<real>(s->rc.grid, s->ph.gamma, method, s->state.template as<real>(), d_out, s->stream);
+    return true;
+}
+
+void displayInto(hgpu_solver* h, int method, float* d_out) {
+    if (method < 0 || method >= hgpu::displayCount(h->s->dim()))
+        throw hgpu::ConfigError(HGPU_ERR_ARG, "display method out of range for this dimension");
+    if (!displayAs<double>(h->s.get(), method, d_out)) displayAs<float>(h->s.get(), method, d_out);
+    hgpu::cudaCheck(cudaGetLastError(), "display launch");
+}
+}  // namespace
+}  // extern "C++"
+
+int hgpu_display_device(hgpu_solver* h, int method, void* d_out) {
+    if (!h || !d_out) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        displayInto(h, method, static_cast<float*>(d_out));
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_display(hgpu_solver* h, int method, float* host_out, size_t count) {
+    if (!h || !host_out) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        const size_t V = h->s->volume();
+        if (count != V) throw hgpu::ConfigError(HGPU_ERR_ARG, "display needs one float per cell");
+        if (!h->display.get()) h->display = hgpu::DeviceBuffer(sizeof(float) * V, false);
+        displayInto(h, method, h->display.as<float>());
+        hgpu::cudaCheck(cudaMemcpyAsync(host_out, h->display.get(), sizeof(float) * V, cudaMemcpyDeviceToHost,
+                                        h->s->stream),
+                        "display download");
+        hgpu::cudaCheck(cudaStreamSynchronize(h->s->stream), "display sync");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_save_fits(hgpu_solver* h, const char* directory, int* save_index) {
+    if (!h || !directory) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        const int dim = h->s->dim(), N = h->s->numStates();
+        const size_t V = h->s->volume();
+        std::vector<std::string> names = {"DENSITY", "MOMENTUM_X"};
+        if (dim > 1) names.push_back("MOMENTUM_Y");
+        if (dim > 2) names.push_back("MOMENTUM_Z");
+        names.push_back("ENERGY_TOTAL");
+        names.push_back("potential");                   // SelfGravitationBehavior::getSaveChannelNames
+        std::string dir(directory);
+        if (!dir.empty() && dir.back() != '/') dir += '/';
+        int index = -1;
+        for (int i = 0; i < 1000000 && index < 0; ++i)   // Solver::getSaveIndex
+            if (!hgpu::fileExists(dir + names[0] + std::to_string(i) + ".fits")) index = i;
+        if (index < 0) throw hgpu::ConfigError(HGPU_ERR_ARG, "no free save index");
+        const bool f32 = dynamic_cast<hgpu::Solver<float>*>(h->s.get()) != nullptr;
+        std::vector<double> d(f32 ? 0 : V * N);
+        std::vector<float> f(f32 ? V * N : 0), plane(V);
+        if (f32) h->s->readState(f.data(), V * N);
+        else h->s->readState(d.data(), V * N);
+        int S[3] = {1, 1, 1};
+        if (auto* s = dynamic_cast<hgpu::Solver<double>*>(h->s.get())) for (int i = 0; i < 3; ++i) S[i] = s->rc.grid.S[i];
+        if (auto* s = dynamic_cast<hgpu::Solver<float>*>(h->s.get())) for (int i = 0; i < 3; ++i) S[i] = s->rc.grid.S[i];
+        for (int ch = 0; ch < (int)names.size(); ++ch) {
+            for (size_t c = 0; c < V; ++c)
+                plane[c] = ch < N ? (f32 ? f[c * N + ch] : (float)d[c * N + ch]) : 0.f;
+            hgpu::writeFitsFloat(dir + names[ch] + std::to_string(index) + ".fits", plane.data(), S[0], S[1], S[2]);
+        }
+        if (save_index) *save_index = index;
         return (int)HGPU_OK;
     });
 }

@@ -74,6 +74,11 @@ template <typename real>
 void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
                     unsigned* health, int hll, cudaStream_t st);
 
+// ---- display scalar (display.cu, convertToTex): method = the reference's DISPLAY_* index ----
+int displayCount(int dim);
+template <typename real>
+void launchDisplay(const Grid& g, real gamma, int method, const real* state, float* out, cudaStream_t st);
+
 // ---- tableaus (combine.cu): alpha/beta in double, order ----
 int tableauOrder(int integrator);
 double tableauAlpha(int integrator, int m, int k);

@@ -228,6 +228,22 @@ int hgpu_profile_update(hgpu_solver* s, int nsteps, hgpu_kernel_time* out, int c
 int hgpu_host_alloc(size_t bytes, void** ptr);
 int hgpu_host_free(void* ptr);
 
+/* ---- output ----
+ * The display scalar of every cell (ghosts included), as the reference's
+ * convertToTex (res/EulerMHDCommon.cl:4-116) computes it for its texture, into a
+ * headless buffer: one float per cell.  `method` is the reference's DISPLAY_* index,
+ * numbered per dimension (src/Equation/Euler.cpp:18-27): DENSITY, VELOCITY,
+ * VELOCITY_X, [VELOCITY_Y], [VELOCITY_Z], PRESSURE, ENERGY_INTERNAL, ENERGY_KINETIC,
+ * ENERGY_TOTAL, POTENTIAL (7 + dim methods). */
+int hgpu_display(hgpu_solver* s, int method, float* host_out, size_t count);
+/* Same into a caller-owned DEVICE array of volume floats, queued on the solver's stream. */
+int hgpu_display_device(hgpu_solver* s, int method, void* d_out);
+/* Solver::save (src/Solver/Solver.cpp:549-589): one FITS file per channel
+ * (DENSITY, MOMENTUM_X.., ENERGY_TOTAL, potential) named <channel><index>.fits in
+ * `directory`, index = the first one whose DENSITY file does not exist; 32-bit
+ * float images of size[0] x size[1] x size[2]. */
+int hgpu_save_fits(hgpu_solver* s, const char* directory, int* save_index);
+
 /* ---- batches of independent problems ----
  * No reference counterpart: the reference runs one problem per process
  * (src/HydroGPUApp.cpp:330-349).  A batch holds problems of the same solver, dim,

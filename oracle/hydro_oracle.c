@@ -146,6 +146,12 @@ int oracle_update(oracle_handle* h, int nsteps, double* last_dt, int* nonfinite)
     return HGPU_OK;
 }
 
+/* The display scalar of every cell (convertToTex); method = the reference's DISPLAY_* index. */
+int oracle_display(oracle_handle* h, int method, float* out) {
+    if (!h || !out) return HGPU_ERR_ARG;
+    return h->d ? display_f64(h->d, method, out) : display_f32(h->f, method, out);
+}
+
 /* Copy an internal buffer out (per-kernel checks): "eigenvalues", "flux", "dt". */
 size_t oracle_get_buffer(oracle_handle* h, const char* name, void* out, size_t cap) {
     size_t n = 0;

@@ -659,6 +659,46 @@ static void FN(hllFlux)(FN(osolver) * s) {
     }
 }
 
+/* ---------------- convertToTex (EulerMHDCommon.cl:4-116): the display scalar ----------------
+ * `method` is the reference's DISPLAY_* index, whose numbering depends on dim
+ * (Euler.cpp:18-27): DENSITY, VELOCITY, VELOCITY_X, [VELOCITY_Y], [VELOCITY_Z],
+ * PRESSURE, ENERGY_INTERNAL, ENERGY_KINETIC, ENERGY_TOTAL, POTENTIAL.  Every cell,
+ * ghosts included; the float4's x component. */
+static int FN(display)(FN(osolver) * s, int method, float* out) {
+    const int N = s->N, E = N - 1, D = s->dim;
+    const REAL g = s->gamma;
+    int kind = method;                       /* 0..9 in the dim-3 numbering */
+    if (method < 0 || method >= 7 + D) return HGPU_ERR_ARG;
+    if (method >= 2 + D) kind = method + (3 - D);
+    FOR_CELLS(s) {
+        long index = IDX(s, x, y, z);
+        const REAL* st = s->state + N * index;
+        REAL density = st[0];
+        REAL v[4];
+        for (int k = 0; k < 4; ++k) v[k] = (k < D ? st[1 + k] : (REAL)0.f) / density;
+        REAL energyTotal = st[E];
+        REAL velocitySq = DOT4(v, v);
+        REAL energyKinetic = .5 * density * velocitySq;
+        REAL energyPotential = density * s->potential[index];
+        REAL energyInternal = energyTotal - energyKinetic - energyPotential;
+        REAL value = 0;
+        switch (kind) {
+        case 0: value = density; break;
+        case 1: value = sqrt(velocitySq); break;
+        case 2: value = v[0]; break;
+        case 3: value = v[1]; break;
+        case 4: value = v[2]; break;
+        case 5: value = (g - 1.) * energyInternal; break;
+        case 6: value = energyInternal; break;
+        case 7: value = energyKinetic; break;
+        case 8: value = energyTotal; break;
+        case 9: value = s->potential[index]; break;
+        }
+        out[index] = (float)value;
+    }
+    return HGPU_OK;
+}
+
 /* ---------------- calcFluxDeriv (CalcFluxDeriv.cl:7-44) ---------------- */
 static void FN(calcFluxDeriv)(FN(osolver) * s, REAL* deriv) {
     const int N = s->N, D = s->dim;

@@ -140,6 +140,11 @@ class Oracle(_Base):
         self.nonfinite = bool(bad.value)
         return dt.value
 
+    def display(self, method):
+        """convertToTex restated: the display scalar of every cell (DISPLAY_* index)."""
+        lib().oracle_display.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        return _display(lib().oracle_display, self.h, _abi.config_volume(self.cfg), method)
+
     def get_buffer(self, name):
         n = lib().oracle_get_buffer(self.h, name.encode(), None, 0)
         a = np.empty(n, dtype=self._np())
@@ -179,6 +184,14 @@ def _refcl_lib(path):
     return _refcl_libs[path]
 
 
+def _display(fn, h, count, method):
+    out = np.empty(count, dtype=np.float32)
+    st = fn(h, int(method), out.ctypes.data)
+    if st:
+        raise ValueError("display method %r: status %d" % (method, st))
+    return out
+
+
 class Refcl(_Base):
     """The reference's kernels compiled for the CPU (one active handle per variant library)."""
 
@@ -216,6 +229,11 @@ class Refcl(_Base):
         self.L.refcl_update(self.h, int(nsteps), ctypes.byref(dt))
         self.last_dt = dt.value
         return dt.value
+
+    def display(self, method):
+        """convertToTex of every cell (the reference's DISPLAY_* index)."""
+        self.L.refcl_display.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        return _display(self.L.refcl_display, self.h, _abi.config_volume(self.cfg), method)
 
     def get_buffer(self, name):
         n = self.L.refcl_get_buffer(self.h, name.encode(), None, 0)

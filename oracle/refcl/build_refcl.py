@@ -53,7 +53,7 @@ def rewrite(text, const_inits):
     text = re.sub(r"\b__global\b", "", text)
     text = re.sub(r"\b__local\b", "", text)
     text = re.sub(r"\b__const\b", "const", text)
-    text = re.sub(r"\((int4|int2|real4)\)\s*\(", r"make_\1(", text)
+    text = re.sub(r"\((int4|int2|real4|float4)\)\s*\(", r"make_\1(", text)
     text = re.sub(r"(\w+)\.xy\s*=\s*\1\.yx\s*;", r"refcl_swap_xy(\1);", text)
     text = re.sub(r"(\w+)\.xz\s*=\s*\1\.zx\s*;", r"refcl_swap_xz(\1);", text)
 
@@ -91,6 +91,13 @@ def generate(ref):
             src = f.read()
         with open(os.path.join(GEN, "include", "HydroGPU", name), "w") as f:
             f.write(rewrite(src, []))
+    # the scalar display kernel (convertToTex) alone: the rest of the file draws vector-field geometry
+    with open(os.path.join(res, "EulerMHDCommon.cl")) as f:
+        src = f.read()
+    display = src[src.index("__kernel void convertToTex("):src.index("constant float2 offset[6]")]
+    with open(os.path.join(GEN, "EulerDisplay.cl.inc"), "w") as f:
+        f.write("/* convertToTex of res/EulerMHDCommon.cl, rewritten (see oracle/refcl/build_refcl.py) */\n")
+        f.write(re.sub(r"\bglobal\b", "", rewrite(display, const_inits)))   # `global` without underscores here
     with open(os.path.join(GEN, "include", "HydroGPU", "Shared", "Common.h"), "w") as f:
         f.write(SHIM_COMMON_H)
     for solver, dim, prec in VARIANTS:
@@ -141,6 +148,12 @@ def program_source(solver, dim, prec, const_inits):
         lines += ['#include "EulerHLLC.cl.inc"', '#include "SelfGravitation.cl.inc"']
     else:
         lines += ['#include "EulerHLL.cl.inc"', '#include "SelfGravitation.cl.inc"']
+    display = ["DENSITY", "VELOCITY", "VELOCITY_X"] + (["VELOCITY_Y"] if dim > 1 else []) + \
+        (["VELOCITY_Z"] if dim > 2 else []) + ["PRESSURE", "ENERGY_INTERNAL", "ENERGY_KINETIC", "ENERGY_TOTAL",
+                                               "POTENTIAL"]
+    lines.append("enum {\n" + "".join("\tDISPLAY_%s,\n" % d for d in display) + "\tNUM_DISPLAY\n};")
+    lines += ["#define DISPLAY_NONE -1", "#ifndef gamma", "#define gamma idealGas_heatCapacityRatio", "#endif",
+              '#include "EulerDisplay.cl.inc"']
     names = sorted(set(const_inits))
     lines.append("static void refcl_init_constants() { %s }" % " ".join("refcl_init_%s();" % c for c in names))
     lines.append('#include "refcl_driver.inc"')

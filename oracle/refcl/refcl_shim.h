@@ -35,7 +35,15 @@ struct int2 {
     int& operator[](int i) { return (&x)[i]; }
 };
 
+struct float4 {
+    float x, y, z, w;
+};
+
 static inline real4 make_real4(real a, real b, real c, real d) { real4 r = {a, b, c, d}; return r; }
+static inline float4 make_float4(double a, double b, double c, double d) {
+    float4 r = {(float)a, (float)b, (float)c, (float)d};
+    return r;
+}
 static inline int4 make_int4(long a, long b, long c, long d) { int4 r = {(int)a, (int)b, (int)c, (int)d}; return r; }
 static inline int2 make_int2(long a, long b) { int2 r = {(int)a, (int)b}; return r; }
 

@@ -73,3 +73,12 @@ def test_initial_conditions_shapes_and_ranges():
     probs = ic.random_quadrant_problems(64, seed=2)
     sides = [p["side"] for p in probs]
     assert min(sides) >= 32 and max(sides) <= 512 and all(s % 16 == 0 for s in sides)
+
+
+def test_display_names():
+    assert _abi.display_names(1) == ["DENSITY", "VELOCITY", "VELOCITY_X", "PRESSURE", "ENERGY_INTERNAL",
+                                     "ENERGY_KINETIC", "ENERGY_TOTAL", "POTENTIAL"]
+    assert len(_abi.display_names(3)) == 10
+    assert _abi.display_index(2, "pressure") == 4
+    with pytest.raises(ValueError):
+        _abi.display_index(1, "VELOCITY_Y")

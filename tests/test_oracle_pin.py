@@ -68,3 +68,20 @@ def test_pin_gamma_five_thirds(refcl):
     cfg = _abi.make_config(solver="EulerHLLC", size=(9, 8, 7), xmin=(0, 0, 0), xmax=(1, 1, 1), gamma=5. / 3.,
                            boundary="MIRROR", integrator="RungeKutta2TVD", cfl=.4)
     pin(refcl, cfg, random_state(cfg, seed=2), steps=3)
+
+
+@pytest.mark.parametrize("solver", ["EulerRoe", "EulerHLLC", "EulerHLL"])
+@pytest.mark.parametrize("dim,prec", [(1, 0), (2, 0), (3, 0), (2, 1), (3, 1)])
+def test_pin_display(refcl, solver, dim, prec):
+    """The display scalar (convertToTex, res/EulerMHDCommon.cl:4-116) restated in the
+    oracle against the reference's own kernel, every display method."""
+    cfg = _abi.make_config(solver=solver, size=SMALL[dim], boundary="PERIODIC", integrator="RungeKutta2",
+                           precision=prec)
+    init = random_state(cfg, seed=dim + 9)
+    o, r = refcl.Oracle(cfg), refcl.Refcl(cfg)
+    o.set_state(init)
+    r.set_state(init)
+    o.update(1)
+    r.update(1)
+    for m in range(len(_abi.display_names(dim))):
+        assert np.array_equal(o.display(m), r.display(m), equal_nan=True), m
