@@ -438,7 +438,8 @@ void Roe<real>::calcFlux(real* stage) {                      // Roe::calcDeriv (
         launchRoeDeltaQ<real>(this->rc.grid, stage, basis.template as<real>(), deltaQTilde.template as<real>(), seam,
                               this->stream);
     });
-    this->launch("roe_flux", 1, [&] {
+    // FP64: per-wave corrections, then the transforms (two kernels, roe.cu)
+    this->launch("roe_flux", sizeof(real) == 8 ? 2 : 1, [&] {
         launchRoeFlux<real>(this->rc.grid, this->rc.cfg.limiter, stage, basis.template as<real>(),
                             deltaQTilde.template as<real>(), this->sc(), this->flux.template as<real>(), seam,
                             this->stream);

@@ -79,6 +79,29 @@ __global__ void __launch_bounds__(kThreads) roeFluxKernel(Grid g, int lim, const
     roeFluxCell<real, D, LIM>(g, lim, *sc, stage, basis, dq, flux, c, x, y, z);
 }
 
+template <int D, int LIM>
+__global__ void __launch_bounds__(kThreads) roeFluxCorrKernel(Grid g, int lim, const double* __restrict__ basis,
+                                                              const double* __restrict__ dq,
+                                                              const StepConst<double>* __restrict__ sc,
+                                                              double* __restrict__ flux) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    roeFluxCorrectionsCell<D, LIM>(g, lim, *sc, basis, dq, flux, c, x, y, z);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) roeFluxXformKernel(Grid g, const double* __restrict__ stage,
+                                                               const double* __restrict__ basis,
+                                                               double* __restrict__ flux) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    roeFluxTransformsCell<D>(g, stage, basis, flux, c, x, y, z);
+}
+
 }  // namespace
 
 // REF: faces along [2, S-2] (res/EulerRoe.cl:27-34, res/Roe.cl:88-95); SEAM: [1, S-1].
@@ -115,9 +138,30 @@ void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* 
     else roeDeltaQKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
 }
 
+template <int LIM>
+void launchRoeFluxSplit(const Grid& g, int limiter, const double* stage, const double* basis, const double* dq,
+                        const StepConst<double>* sc, double* flux, cudaStream_t st) {
+    if (g.dim == 1) {
+        roeFluxCorrKernel<1, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux);
+        roeFluxXformKernel<1><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, flux);
+    } else if (g.dim == 2) {
+        roeFluxCorrKernel<2, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux);
+        roeFluxXformKernel<2><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, flux);
+    } else {
+        roeFluxCorrKernel<3, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux);
+        roeFluxXformKernel<3><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, flux);
+    }
+}
+
 template <typename real, int LIM>
 void launchRoeFluxLim(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
                       const StepConst<real>* sc, real* flux, cudaStream_t st) {
+    // FP64 runs the flux as two lighter passes (more resident warps, same bits)
+    if (sizeof(real) == 8) {
+        launchRoeFluxSplit<LIM>(g, limiter, (const double*)stage, (const double*)basis, (const double*)dq,
+                                (const StepConst<double>*)sc, (double*)flux, st);
+        return;
+    }
     if (g.dim == 1) roeFluxKernel<real, 1, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
     else if (g.dim == 2) roeFluxKernel<real, 2, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
     else roeFluxKernel<real, 3, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);

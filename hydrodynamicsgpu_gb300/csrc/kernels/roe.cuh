@@ -304,4 +304,60 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
     rightTransform<real, D, SIDE>(rec, ft, F);
 }
 
+
+// The FP64 flux in two passes (same operations, same bits as roeFlux):
+//   pass 1, per wave i: corr_i = (lambda_i dq_i / 2) (theta_i + phi(r_i) (eps_i - theta_i))
+//   pass 2: ft = lambda (L avg) - corr, F = R ft
+// Each pass keeps far fewer values live than the fused form, so more warps fit per SM.
+// REC also stores the per-wave tape values of this pass (A, phi, phi', r; the caller
+// offsets tape to the face, as for roeFlux).
+template <int D, int SIDE, int LIM, bool REC = false>
+__device__ __forceinline__ void roeFluxCorrections(const double* rec, const double* dqL, const double* dq,
+                                                   const double* dqR, double dt_dx, int lim, double* corr,
+                                                   double* __restrict__ tape = nullptr, long long V = 0) {
+    typedef RoeRec<D> R_;
+    const int N = D + 2;
+    const double vx = rec[R_::VX];
+    const bool midUp = geZero(vx);
+    const double midTheta = midUp ? 1. : -1.;
+    const double midEpsTheta = mulI(vx, dt_dx) - midTheta;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const bool mid = i > 0 && i < N - 1;
+        const double eigenvalue = roeEigenvalue<double, D>(rec, i);
+        const bool up = mid ? midUp : geZero(eigenvalue);
+        const double rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
+        const double theta = mid ? midTheta : (up ? 1. : -1.);
+        const double phi = slopeLimiter<double>(LIM >= 0 ? LIM : lim, rTilde);
+        const double epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
+        const double A = theta + phi * epsMinusTheta;
+        corr[i] = halfOf(mulI(eigenvalue, dq[i])) * A;
+        if (REC) {
+            tape[((long long)FT_A * N + i) * V] = A;
+            tape[((long long)FT_PHI * N + i) * V] = phi;
+            tape[((long long)FT_DPHI * N + i) * V] = limiterDual(LIM >= 0 ? LIM : lim, Dual{rTilde, 1.}).d;
+            tape[((long long)FT_R * N + i) * V] = rTilde;
+        }
+    }
+}
+
+// REC also stores the tape values of this pass (L avg, and ft after the correction)
+template <int D, int SIDE, bool REC = false>
+__device__ __forceinline__ void roeFluxTransforms(const double* rec, const double* sL, const double* sR,
+                                                  const double* corr, double* F, double* __restrict__ tape = nullptr,
+                                                  long long V = 0) {
+    const int N = D + 2;
+    double avg[5], ft[5];
+#pragma unroll
+    for (int i = 0; i < N; ++i) avg[i] = halfOf(sR[i] + sL[i]);
+    leftTransform<double, D, SIDE>(rec, avg, ft);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if (REC) tape[((long long)FT_Y * N + i) * V] = ft[i];
+        ft[i] = ft[i] * roeEigenvalue<double, D>(rec, i) - corr[i];
+        if (REC) tape[((long long)FT_F * N + i) * V] = ft[i];
+    }
+    rightTransform<double, D, SIDE>(rec, ft, F);
+}
+
 }  // namespace hgpu

@@ -164,4 +164,64 @@ __device__ __forceinline__ void roeFluxCell(const Grid& g, int lim, const StepCo
         fluxFace<real, D, (D > 2 ? 2 : 0), LIM, REC>(g, lim, sc.dt_dx[2], stage, basis, dq, flux, c, sR, tape);
 }
 
+
+// the two passes of the split FP64 flux (roe.cuh) over the faces of one cell
+// (REC: tape planes per face as for roeFluxCell)
+template <int D, int LIM, bool REC = false>
+__device__ __forceinline__ void roeFluxCorrectionsCell(const Grid& g, int lim, const StepConst<double>& sc,
+                                                       const double* __restrict__ basis,
+                                                       const double* __restrict__ dq, double* __restrict__ flux,
+                                                       long long c, int x, int y, int z,
+                                                       double* __restrict__ tape = nullptr) {
+    const int N = D + 2, NB = RoeRec<D>::NB;
+#pragma unroll
+    for (int side = 0; side < D; ++side) {
+        if (!roeFace(g, side, x, y, z, 2, 1)) continue;
+        const long long st = g.step[side];
+        double rec[NB], qL[N], q[N], qR[N], corr[N];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)side * NB + k) * g.V + c];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const double* p = dq + ((long long)side * N + i) * g.V + c;
+            qL[i] = p[-st];
+            q[i] = p[0];
+            qR[i] = p[st];
+        }
+        double* tf = REC ? tape + (long long)side * FT_PLANES * N * g.V + c : nullptr;
+        if (side == 0) roeFluxCorrections<D, 0, LIM, REC>(rec, qL, q, qR, sc.dt_dx[0], lim, corr, tf, g.V);
+        else if (side == 1)
+            roeFluxCorrections<D, (D > 1 ? 1 : 0), LIM, REC>(rec, qL, q, qR, sc.dt_dx[1], lim, corr, tf, g.V);
+        else roeFluxCorrections<D, (D > 2 ? 2 : 0), LIM, REC>(rec, qL, q, qR, sc.dt_dx[2], lim, corr, tf, g.V);
+#pragma unroll
+        for (int i = 0; i < N; ++i) flux[((long long)side * N + i) * g.V + c] = corr[i];
+    }
+}
+
+template <int D, bool REC = false>
+__device__ __forceinline__ void roeFluxTransformsCell(const Grid& g, const double* __restrict__ stage,
+                                                      const double* __restrict__ basis, double* __restrict__ flux,
+                                                      long long c, int x, int y, int z,
+                                                      double* __restrict__ tape = nullptr) {
+    const int N = D + 2, NB = RoeRec<D>::NB;
+    double sR[N];
+    loadState<double, D>(stage, c, sR);
+#pragma unroll
+    for (int side = 0; side < D; ++side) {
+        if (!roeFace(g, side, x, y, z, 2, 1)) continue;
+        double sL[N], rec[NB], corr[N], F[N];
+        loadState<double, D>(stage, c - g.step[side], sL);
+#pragma unroll
+        for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)side * NB + k) * g.V + c];
+#pragma unroll
+        for (int i = 0; i < N; ++i) corr[i] = flux[((long long)side * N + i) * g.V + c];
+        double* tf = REC ? tape + (long long)side * FT_PLANES * N * g.V + c : nullptr;
+        if (side == 0) roeFluxTransforms<D, 0, REC>(rec, sL, sR, corr, F, tf, g.V);
+        else if (side == 1) roeFluxTransforms<D, (D > 1 ? 1 : 0), REC>(rec, sL, sR, corr, F, tf, g.V);
+        else roeFluxTransforms<D, (D > 2 ? 2 : 0), REC>(rec, sL, sR, corr, F, tf, g.V);
+#pragma unroll
+        for (int j = 0; j < N; ++j) flux[((long long)side * N + j) * g.V + c] = F[j];
+    }
+}
+
 }  // namespace hgpu

@@ -1,6 +1,6 @@
-// roe_record.cu -- the Roe flux kernel that also records, per face and wave, the
-// values the adjoint's flux VJP reads back (roe.cuh FT_* planes).  The flux it writes
-// is bit-identical to roeFluxKernel's (same code, extra stores).  FP64 only.
+// roe_record.cu -- the Roe flux kernels that also record, per face and wave, the
+// values the adjoint's flux VJP reads back (roe.cuh FT_* planes).  The flux they
+// write is bit-identical to the production FP64 flux's (same code, extra stores).
 #include "../../../include/hgpu/hgpu.h"
 #include "kernels.h"
 #include "roe_cells.cuh"
@@ -10,26 +10,45 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// two passes, as the production FP64 flux runs (roe.cu): the per-wave corrections
+// (recording A, phi, phi', r), then the transforms (recording L avg and ft)
 template <int D, int LIM>
-__global__ void __launch_bounds__(kThreads) roeFluxRecordKernel(Grid g, int lim, const double* __restrict__ stage,
-                                                                const double* __restrict__ basis,
-                                                                const double* __restrict__ dq,
-                                                                const StepConst<double>* __restrict__ sc,
-                                                                double* __restrict__ flux, double* __restrict__ tape) {
+__global__ void __launch_bounds__(kThreads) roeFluxCorrRecordKernel(Grid g, int lim,
+                                                                    const double* __restrict__ basis,
+                                                                    const double* __restrict__ dq,
+                                                                    const StepConst<double>* __restrict__ sc,
+                                                                    double* __restrict__ flux,
+                                                                    double* __restrict__ tape) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    roeFluxCell<double, D, LIM, true>(g, lim, *sc, stage, basis, dq, flux, c, x, y, z, tape);
+    roeFluxCorrectionsCell<D, LIM, true>(g, lim, *sc, basis, dq, flux, c, x, y, z, tape);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) roeFluxXformRecordKernel(Grid g, const double* __restrict__ stage,
+                                                                     const double* __restrict__ basis,
+                                                                     double* __restrict__ flux,
+                                                                     double* __restrict__ tape) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    roeFluxTransformsCell<D, true>(g, stage, basis, flux, c, x, y, z, tape);
 }
 
 template <int LIM>
 void launchLim(const Grid& g, int lim, const double* stage, const double* basis, const double* dq,
                const StepConst<double>* sc, double* flux, double* tape, cudaStream_t st) {
     const unsigned blocks = (unsigned)((g.V + kThreads - 1) / kThreads);
-    if (g.dim == 1) roeFluxRecordKernel<1, LIM><<<blocks, kThreads, 0, st>>>(g, lim, stage, basis, dq, sc, flux, tape);
-    else if (g.dim == 2) roeFluxRecordKernel<2, LIM><<<blocks, kThreads, 0, st>>>(g, lim, stage, basis, dq, sc, flux, tape);
-    else roeFluxRecordKernel<3, LIM><<<blocks, kThreads, 0, st>>>(g, lim, stage, basis, dq, sc, flux, tape);
+#define L(DD)                                                                                            \
+    roeFluxCorrRecordKernel<DD, LIM><<<blocks, kThreads, 0, st>>>(g, lim, basis, dq, sc, flux, tape);      \
+    roeFluxXformRecordKernel<DD><<<blocks, kThreads, 0, st>>>(g, stage, basis, flux, tape)
+    if (g.dim == 1) { L(1); }
+    else if (g.dim == 2) { L(2); }
+    else { L(3); }
+#undef L
 }
 }  // namespace
 
