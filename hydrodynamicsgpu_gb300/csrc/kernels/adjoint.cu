@@ -188,8 +188,9 @@ __device__ __forceinline__ void stageCotangent(const AdjStage& st, long long c, 
     }
 }
 
+// (3 blocks per SM: the register cap's few spills cost less than the occupancy gained)
 template <int D>
-__global__ void __launch_bounds__(kT) adjFluxKernel(Grid g, Phys<double> ph, int lim, double k0, double k1, double k2,
+__global__ void __launch_bounds__(kT, 3) adjFluxKernel(Grid g, Phys<double> ph, int lim, double k0, double k1, double k2,
                                                     const double* __restrict__ U, const double* __restrict__ DQ,
                                                     const double* __restrict__ B, const double* __restrict__ FT,
                                                     AdjStage st, AdjScratch S, int first) {
