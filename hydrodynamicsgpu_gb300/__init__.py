@@ -30,6 +30,8 @@ SIGNATURES = {
     "hgpu_get_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_size_t)]),
     "hgpu_set_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    "hgpu_set_state_potential": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P, ctypes.c_size_t]),
+    "hgpu_get_potential": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     "hgpu_get_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     "hgpu_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_step": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
@@ -198,11 +200,28 @@ class Solver:
     def name(self):
         return "EulerRoe" if self.cfg.solver == 0 else "EulerHLLC"
 
-    def resetState(self, state):
+    def resetState(self, state, potential=None):
+        """Solver::resetState's upload (Converter::toGPU + SelfGravitation::resetState):
+        ``potential`` is the initial conditions' potential channel (one value per cell),
+        or None for zero.  With use_gravity the potential starts as -density instead."""
         a = np.ascontiguousarray(state, dtype=self.dtype).reshape(-1)
         if a.size != self.count:
             raise ValueError("state has %d elements, solver needs %d" % (a.size, self.count))
-        check(lib().hgpu_set_state(self.h, a.ctypes.data, a.size))
+        if potential is None:
+            check(lib().hgpu_set_state(self.h, a.ctypes.data, a.size))
+            return
+        p = np.ascontiguousarray(potential, dtype=self.dtype).reshape(-1)
+        if p.size != self.volume:
+            raise ValueError("potential has %d elements, solver needs %d" % (p.size, self.volume))
+        check(lib().hgpu_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size))
+
+    def getPotential(self, out=None):
+        """The gravitational potential (one value per cell, ghosts included)."""
+        a = out if out is not None else np.empty(self.volume, dtype=self.dtype)
+        check(lib().hgpu_get_potential(self.h, a.ctypes.data, a.size))
+        return a
+
+    get_potential = getPotential
 
     set_state = resetState
 

@@ -44,7 +44,10 @@ class HgpuConfig(ctypes.Structure):
         ("integrator", ctypes.c_int),
         ("precision", ctypes.c_int),
         ("compat", ctypes.c_int),
-        ("reserved", ctypes.c_int * 8),
+        ("use_gravity", ctypes.c_int),
+        ("gauss_seidel_max_iter", ctypes.c_int),
+        ("gravitational_constant", ctypes.c_double),
+        ("reserved", ctypes.c_int * 4),
     ]
 
 
@@ -62,13 +65,17 @@ def _index(name, table, what):
 
 def make_config(solver="EulerRoe", size=(256, 256), xmin=(-.5, -.5, -.5), xmax=(.5, .5, .5), gamma=1.4,
                 cfl=.5, use_fixed_dt=False, fixed_dt=.001, boundary="FREEFLOW", limiter="Superbee",
-                integrator="ForwardEuler", precision=FP64, compat=COMPAT_REF, dim=0):
+                integrator="ForwardEuler", precision=FP64, compat=COMPAT_REF, dim=0, use_gravity=False,
+                gauss_seidel_max_iter=20, gravitational_constant=1.):
     """Build an HgpuConfig from the reference's config key values.
 
     ``size`` lists cells per axis including the 2 ghost layers per side (the
     reference's ``size`` key); missing axes are 1.  ``boundary`` is one name for
     every side, or a sequence of per-axis ``{"min": name, "max": name}`` dicts /
-    ``(min, max)`` pairs (the reference's ``boundaryMethods`` table)."""
+    ``(min, max)`` pairs (the reference's ``boundaryMethods`` table).
+    ``use_gravity``, ``gauss_seidel_max_iter`` and ``gravitational_constant`` are
+    the ``useGravity``, ``gaussSeidelMaxIter`` and ``defs.selfGrav_gravitationalConstant``
+    keys (res/config.lua:65-74)."""
     cfg = HgpuConfig()
     cfg.solver = _index(solver, SOLVERS, "solver")
     cfg.dim = dim
@@ -95,6 +102,9 @@ def make_config(solver="EulerRoe", size=(256, 256), xmin=(-.5, -.5, -.5), xmax=(
     cfg.integrator = _index(integrator, INTEGRATORS, "integrator")
     cfg.precision = int(precision)
     cfg.compat = int(compat)
+    cfg.use_gravity = int(bool(use_gravity))
+    cfg.gauss_seidel_max_iter = int(gauss_seidel_max_iter)
+    cfg.gravitational_constant = float(gravitational_constant)
     return cfg
 
 

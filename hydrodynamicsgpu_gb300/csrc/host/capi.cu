@@ -132,6 +132,9 @@ int hgpu_config_default(hgpu_config* cfg) {
     cfg->integrator = HGPU_INTEGRATOR_FORWARD_EULER;
     cfg->precision = HGPU_FP64;
     cfg->compat = HGPU_COMPAT_REF;
+    cfg->use_gravity = 0;                      // config.lua:65
+    cfg->gauss_seidel_max_iter = 20;           // config.lua:68
+    cfg->gravitational_constant = 1.;          // config.lua:74
     return HGPU_OK;
 }
 
@@ -171,8 +174,25 @@ int hgpu_get_shape(const hgpu_solver* h, int* dim, int* num_states, size_t* volu
 }
 
 int hgpu_set_state(hgpu_solver* h, const void* host_state, size_t count) {
+    return hgpu_set_state_potential(h, host_state, count, nullptr, 0);
+}
+
+int hgpu_set_state_potential(hgpu_solver* h, const void* host_state, size_t count, const void* host_potential,
+                             size_t potential_count) {
     if (!h || !host_state) return fail(HGPU_ERR_ARG, "null argument");
-    return guarded([&]() { h->s->resetState(host_state, count); return (int)HGPU_OK; });
+    if (host_potential && potential_count != h->s->volume())
+        return fail(HGPU_ERR_ARG, "potential element count mismatch");
+    return guarded([&]() {
+        const bool wasLive = h->s->potentialLive();
+        h->s->resetState(host_state, count, host_potential);
+        if (h->s->potentialLive() != wasLive) destroyGraph(h);   // the step's kernels differ
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_get_potential(hgpu_solver* h, void* host_potential, size_t count) {
+    if (!h || !host_potential) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() { h->s->readPotential(host_potential, count); return (int)HGPU_OK; });
 }
 
 int hgpu_get_state(hgpu_solver* h, void* host_state, size_t count) {
@@ -324,6 +344,8 @@ int hgpu_host_free(void* ptr) {
 
 namespace {
 hgpu::RoeAdjoint& adjointOf(hgpu_solver* h) {
+    if (h->s->potentialLive())
+        throw hgpu::ConfigError(HGPU_ERR_UNSUPPORTED, "the adjoint covers a zero gravitational potential");
     if (!h->adjoint) {
         auto* s = dynamic_cast<hgpu::Solver<double>*>(h->s.get());
         if (!s) throw hgpu::ConfigError(HGPU_ERR_UNSUPPORTED, "the adjoint covers EulerRoe in FP64");
@@ -419,6 +441,8 @@ struct hgpu_batch {
 int hgpu_batch_create(const hgpu_config* cfgs, int nproblems, hgpu_batch** out) {
     if (!cfgs || !out || nproblems <= 0) return fail(HGPU_ERR_ARG, "bad argument");
     *out = nullptr;
+    for (int p = 0; p < nproblems; ++p)
+        if (cfgs[p].use_gravity) return fail(HGPU_ERR_UNSUPPORTED, "batched problems run with a zero potential");
     return guarded([&]() {
         std::unique_ptr<hgpu_batch> h(new hgpu_batch());
         h->b = hgpu::createBatch(std::vector<hgpu_config>(cfgs, cfgs + nproblems));
@@ -505,7 +529,8 @@ template <typename real>
 bool displayAs(hgpu::SolverBase* b, int method, float* d_out) {
     auto* s = dynamic_cast<hgpu::Solver<real>*>(b);
     if (!s) return false;
-    hgpu::launchDisplay<real>(s->rc.grid, s->ph.gamma, method, s->state.template as<real>(), d_out, s->stream);
+    hgpu::launchDisplay<real>(s->rc.grid, s->ph.gamma, method, s->state.template as<real>(), d_out, s->stream,
+                              s->potential.template as<real>());
     return true;
 }
 
@@ -560,14 +585,16 @@ int hgpu_save_fits(hgpu_solver* h, const char* directory, int* save_index) {
         const bool f32 = dynamic_cast<hgpu::Solver<float>*>(h->s.get()) != nullptr;
         std::vector<double> d(f32 ? 0 : V * N);
         std::vector<float> f(f32 ? V * N : 0), plane(V);
-        if (f32) h->s->readState(f.data(), V * N);
-        else h->s->readState(d.data(), V * N);
+        std::vector<double> potD(f32 ? 0 : V);
+        std::vector<float> potF(f32 ? V : 0);
+        if (f32) { h->s->readState(f.data(), V * N); h->s->readPotential(potF.data(), V); }
+        else { h->s->readState(d.data(), V * N); h->s->readPotential(potD.data(), V); }
         int S[3] = {1, 1, 1};
         if (auto* s = dynamic_cast<hgpu::Solver<double>*>(h->s.get())) for (int i = 0; i < 3; ++i) S[i] = s->rc.grid.S[i];
         if (auto* s = dynamic_cast<hgpu::Solver<float>*>(h->s.get())) for (int i = 0; i < 3; ++i) S[i] = s->rc.grid.S[i];
         for (int ch = 0; ch < (int)names.size(); ++ch) {
             for (size_t c = 0; c < V; ++c)
-                plane[c] = ch < N ? (f32 ? f[c * N + ch] : (float)d[c * N + ch]) : 0.f;
+                plane[c] = ch < N ? (f32 ? f[c * N + ch] : (float)d[c * N + ch]) : (f32 ? potF[c] : (float)potD[c]);
             hgpu::writeFitsFloat(dir + names[ch] + std::to_string(index) + ".fits", plane.data(), S[0], S[1], S[2]);
         }
         if (save_index) *save_index = index;

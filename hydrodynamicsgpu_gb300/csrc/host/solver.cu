@@ -107,13 +107,19 @@ ResolvedConfig resolveConfig(const hgpu_config& cfg) {
         rc.dx[i] = cfg.compat == HGPU_COMPAT_REF ? bakedDx(d) : d;
         if (i < dim && !(rc.dx[i] > 0)) throw ConfigError(HGPU_ERR_CONFIG, "xmax must exceed xmin");
     }
+    if (cfg.gauss_seidel_max_iter < 0) throw ConfigError(HGPU_ERR_CONFIG, "gauss_seidel_max_iter must be >= 0");
+    if (cfg.use_gravity && cfg.compat != HGPU_COMPAT_REF)
+        throw ConfigError(HGPU_ERR_UNSUPPORTED, "self-gravity is provided with the REF scheme only");
     // `defs` values reach the program through Lua's number formatting (%.14g)
     if (cfg.compat == HGPU_COMPAT_REF) {
         char buf[64];
         std::snprintf(buf, sizeof buf, "%.14g", cfg.gamma);
         rc.gamma = std::strtod(buf, nullptr);
+        std::snprintf(buf, sizeof buf, "%.14g", cfg.gravitational_constant);
+        rc.gravityG = std::strtod(buf, nullptr);
     } else {
         rc.gamma = cfg.gamma;
+        rc.gravityG = cfg.gravitational_constant;
     }
     rc.dim = dim;
     rc.numStates = dim + 2;
@@ -165,6 +171,23 @@ void ForwardEuler<real>::integrateZeroDeriv() {
     Solver<real>* s = this->solver;
     s->boundary();                                            // the callback's solver->boundary()
     s->launch("gravity_pass", 1, [&] { launchZeroAdd<real>(s->rc.grid, s->state.template as<real>(), s->sc(), s->stream); });
+}
+
+// FE: the callback's relaxation and calcGravityDeriv read the state, its boundary()
+// refreshes the ghosts, then state += deriv * dt (the deriv reads interior cells only,
+// so it is formed after the ghost fill, fused with the update)
+template <typename real>
+void ForwardEuler<real>::integrateGravity() {
+    Solver<real>* s = this->solver;
+    if (s->rc.cfg.use_gravity) s->relaxPotential(s->state.template as<real>(), s->rc.cfg.gauss_seidel_max_iter);
+    s->boundary();
+    CombinePlan<real> plan{};
+    plan.fe = 1;
+    plan.slot[0] = s->state.template as<real>();
+    s->launch("gravity_source_combine", 1, [&] {
+        launchGravityCombine<real>(s->rc.grid, s->gc, s->state.template as<real>(), s->potential.template as<real>(),
+                                   plan, s->sc(), s->stream);
+    });
 }
 
 template <typename real>
@@ -253,6 +276,9 @@ void RungeKutta<real>::buildPlans() {
     plans_ = sp.plans;
     inputSlot_ = sp.inputSlot;
     nslots_ = sp.nslots;
+    callbackK_.assign(order_, false);
+    for (int k = 0; k < order_; ++k)
+        for (int m = k; m < order_; ++m) callbackK_[k] = callbackK_[k] || tableauBeta(tableau_, m, k) != 0.0;
     work_.clear();
     size_t bytes = sizeof(real) * (size_t)this->solver->rc.grid.V * this->solver->rc.numStates;
     for (int i = 0; i < nslots_; ++i) work_.emplace_back(bytes, true);
@@ -286,6 +312,23 @@ void RungeKutta<real>::integrateZeroDeriv() {
     });
 }
 
+// RK: the callback of stage k (RungeKutta.h:76-123) relaxes the potential against the
+// stage state's density and forms calcGravityDeriv from it; the deriv goes into this
+// stage's column of the combine.  Its boundary() only touches the stage buffer, which
+// the next stage rebuilds from the saved stage states, so it changes nothing.
+template <typename real>
+void RungeKutta<real>::integrateGravity() {
+    Solver<real>* s = this->solver;
+    for (int k = 0; k < order_; ++k) {
+        real* in = plans_[k].slot[inputSlot_[k]];
+        if (callbackK_[k] && s->rc.cfg.use_gravity) s->relaxPotential(in, s->rc.cfg.gauss_seidel_max_iter);
+        s->launch("gravity_source_combine", 1, [&] {
+            launchGravityCombine<real>(s->rc.grid, s->gc, in, s->potential.template as<real>(), plans_[k], s->sc(),
+                                       s->stream);
+        });
+    }
+}
+
 // ---------------- Solver ----------------
 template <typename real>
 Solver<real>::Solver(const ResolvedConfig& rc_) : rc(rc_) {
@@ -295,6 +338,7 @@ Solver<real>::Solver(const ResolvedConfig& rc_) : rc(rc_) {
     }
     ph.gamma = (real)rc.gamma;
     ph.cfl = rc.cfg.cfl;
+    gc = gravityConst<real>(rc.dx, rc.gravityG, rc.dim);
 }
 
 template <typename real>
@@ -343,13 +387,56 @@ void Solver<real>::initBuffers() {                           // Solver::initBuff
     dtAcc = DeviceBuffer(sizeof(unsigned long long), true);
     healthBuf = DeviceBuffer(sizeof(unsigned), true);
     health = healthBuf.as<unsigned>();
+    potential = DeviceBuffer(sizeof(real) * (size_t)rc.grid.V, true);
+}
+
+// Converter::toGPU (Solver.cpp:333-337) then SelfGravitation::resetState
+// (SelfGravitation.cpp:35-98): the potential is -density with useGravity (relaxed
+// 100 x gaussSeidelMaxIter times), else the initial conditions' channel; the total
+// energy gets the potential as it was before relaxing (the host vector) added.
+template <typename real>
+void Solver<real>::resetState(const void* host, size_t count, const void* pot) {
+    if (count != (size_t)rc.grid.V * rc.numStates) throw ConfigError(HGPU_ERR_ARG, "state element count mismatch");
+    const size_t V = (size_t)rc.grid.V;
+    cudaCheck(cudaMemcpyAsync(state.get(), host, sizeof(real) * count, cudaMemcpyHostToDevice, stream), "set_state");
+    bool nonzero = false;
+    if (!rc.cfg.use_gravity && pot) {
+        const unsigned char* b = static_cast<const unsigned char*>(pot);
+        for (size_t i = 0; i < sizeof(real) * V && !nonzero; ++i) nonzero = b[i] != 0;
+    }
+    if (!rc.cfg.use_gravity && nonzero)
+        cudaCheck(cudaMemcpyAsync(potential.get(), pot, sizeof(real) * V, cudaMemcpyHostToDevice, stream),
+                  "set_potential");
+    else
+        cudaCheck(cudaMemsetAsync(potential.get(), 0, sizeof(real) * V, stream), "zero potential");
+    launchPotentialInit<real>(rc.grid, rc.cfg.use_gravity ? 1 : 0, state.as<real>(), potential.as<real>(), stream);
+    potentialLive_ = rc.cfg.use_gravity || nonzero;
+    if (rc.cfg.use_gravity) {
+        // the relaxation reads the density, which the energy update above does not touch
+        for (int tries = 0; tries < 100; ++tries) relaxPotential(state.as<real>(), rc.cfg.gauss_seidel_max_iter);
+    }
+    cudaCheck(cudaGetLastError(), "reset kernels");
+    cudaCheck(cudaStreamSynchronize(stream), "set_state sync");
 }
 
 template <typename real>
-void Solver<real>::resetState(const void* host, size_t count) {
-    if (count != (size_t)rc.grid.V * rc.numStates) throw ConfigError(HGPU_ERR_ARG, "state element count mismatch");
-    cudaCheck(cudaMemcpyAsync(state.get(), host, sizeof(real) * count, cudaMemcpyHostToDevice, stream), "set_state");
-    cudaCheck(cudaStreamSynchronize(stream), "set_state sync");
+void Solver<real>::relaxPotential(const real* densitySource, int sweeps) {
+    for (int i = 0; i < sweeps; ++i) {
+        launch("potential_boundary", rc.dim, [&] {
+            launchPotentialBoundary<real>(rc.grid, methods, potential.as<real>(), stream);
+        });
+        launch("poisson_relax", 2, [&] {
+            launchRelaxSweep<real>(rc.grid, gc, densitySource, potential.as<real>(), stream);
+        });
+    }
+}
+
+template <typename real>
+void Solver<real>::readPotential(void* host, size_t count) {
+    if (count != (size_t)rc.grid.V) throw ConfigError(HGPU_ERR_ARG, "potential element count mismatch");
+    cudaCheck(cudaMemcpyAsync(host, potential.get(), sizeof(real) * count, cudaMemcpyDeviceToHost, stream),
+              "get_potential");
+    cudaCheck(cudaStreamSynchronize(stream), "get_potential sync");
 }
 
 template <typename real>
@@ -397,7 +484,10 @@ void Solver<real>::update() {                                // Solver::update (
 }
 
 template <typename real>
-void Solver<real>::applyPotential() { integrator->integrateZeroDeriv(); }
+void Solver<real>::applyPotential() {
+    if (potentialLive_) integrator->integrateGravity();
+    else integrator->integrateZeroDeriv();
+}
 
 template <typename real>
 void FiniteVolumeSolver<real>::initBuffers() {               // FiniteVolumeSolver.cpp:10-15
@@ -417,7 +507,7 @@ template <typename real>
 void Roe<real>::initFlux() {                                 // Roe::initFlux (Roe.cpp:82-86)
     this->launch("roe_eigenbasis", 1, [&] {
         launchRoeBasis<real>(this->rc.grid, this->ph, this->state.template as<real>(), basis.template as<real>(),
-                             this->rc.cfg.compat == HGPU_COMPAT_SEAM, this->stream);
+                             this->rc.cfg.compat == HGPU_COMPAT_SEAM, this->stream, this->livePotential());
     });
 }
 
@@ -467,7 +557,7 @@ template <typename real>
 void HLL<real>::initStep() {                                 // HLL::initStep (HLL.cpp:31-33)
     this->launch("hllc_wave_speeds", 1, [&] {
         launchHllcWaves<real>(this->rc.grid, this->ph, this->state.template as<real>(), waves.template as<real>(),
-                              this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream);
+                              this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream, this->livePotential());
     });
 }
 
@@ -487,7 +577,7 @@ void HLL<real>::step() {                                     // HLL::step (HLL.c
         this->launch("hllc_flux", 1, [&] {
             launchHllcFlux<real>(this->rc.grid, this->ph, stage, waves.template as<real>(),
                                  this->flux.template as<real>(), this->health, this->rc.cfg.solver == HGPU_SOLVER_HLL,
-                                 this->stream);
+                                 this->stream, this->livePotential());
         });
     });
 }

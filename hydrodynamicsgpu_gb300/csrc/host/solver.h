@@ -18,6 +18,7 @@
 
 #include "../../../include/hgpu/hgpu.h"
 #include "../kernels/kernels.h"
+#include "../kernels/gravity.h"
 
 namespace hgpu {
 
@@ -58,6 +59,7 @@ struct ResolvedConfig {
     int numStates = 0;
     double dx[3] = {1, 1, 1};   // as baked (6 significant digits in REF mode)
     double gamma = 1.4;         // as baked (%.14g in REF mode)
+    double gravityG = 1.;       // defs.selfGrav_gravitationalConstant as baked (%.14g)
     Grid grid;
 };
 ResolvedConfig resolveConfig(const hgpu_config& cfg);
@@ -104,6 +106,9 @@ public:
     virtual void integrate(const std::function<void(real* stage)>& computeFlux) = 0;
     // the self-gravity pass with a zero potential (SelfGravitation::applyPotential)
     virtual void integrateZeroDeriv() = 0;
+    // the self-gravity pass with a live potential: per callback the relaxation sweeps
+    // (useGravity) and calcGravityDeriv of the stage state (SelfGravitation.cpp:100-124)
+    virtual void integrateGravity() = 0;
     virtual int order() const = 0;
     virtual int extraBuffers() const = 0;
 protected:
@@ -116,6 +121,7 @@ public:
     using Integrator<real>::Integrator;
     void integrate(const std::function<void(real* stage)>& computeFlux) override;
     void integrateZeroDeriv() override;
+    void integrateGravity() override;
     int order() const override { return 1; }
     int extraBuffers() const override { return 0; }
 };
@@ -126,6 +132,7 @@ public:
     RungeKutta(Solver<real>* s, int tableau);
     void integrate(const std::function<void(real* stage)>& computeFlux) override;
     void integrateZeroDeriv() override;
+    void integrateGravity() override;
     int order() const override { return order_; }
     int extraBuffers() const override { return nslots_; }
 private:
@@ -133,6 +140,7 @@ private:
     bool alphaIsBinary_ = true;
     std::vector<CombinePlan<real>> plans_;   // one per stage
     std::vector<int> inputSlot_;             // stage k reads u^(k) from this slot
+    std::vector<bool> callbackK_;            // the reference calls back at stage k (a nonzero beta in column k)
     std::vector<DeviceBuffer> work_;
     void buildPlans();
 };
@@ -142,7 +150,9 @@ class ISolver {
 public:
     virtual ~ISolver() = default;
     virtual void init() = 0;
-    virtual void resetState(const void* host, size_t count) = 0;
+    // Converter::toGPU + SelfGravitation::resetState; potential: the initial conditions'
+    // potential channel (V values) or null for zero
+    virtual void resetState(const void* host, size_t count, const void* potential = nullptr) = 0;
     virtual std::string name() const = 0;
     virtual const Equation& getEquation() const = 0;
 };
@@ -173,6 +183,8 @@ public:
     int launches_ = 0;                     // kernels launched by the last update()
     virtual void update() = 0;
     virtual void readState(void* host, size_t count) = 0;
+    virtual void readPotential(void* host, size_t count) = 0;
+    virtual bool potentialLive() const = 0;
     virtual double lastDt() = 0;
     virtual void* stateDevicePtr() = 0;
     virtual int kernelsPerStep() const = 0;
@@ -189,8 +201,10 @@ public:
     explicit Solver(const ResolvedConfig& rc);
     ~Solver() override;
     void init() override;
-    void resetState(const void* host, size_t count) override;
+    void resetState(const void* host, size_t count, const void* potential = nullptr) override;
     void readState(void* host, size_t count) override;
+    void readPotential(void* host, size_t count) override;
+    bool potentialLive() const override { return potentialLive_; }
     const Equation& getEquation() const override { return *equation; }
     void update() override;                 // Solver::update (Solver.cpp:521-546)
     void boundary();                        // Solver::boundary (Solver.cpp:448-464)
@@ -206,6 +220,11 @@ public:
     ResolvedConfig rc;
     Phys<real> ph;
     DeviceBuffer state, flux, stepConst, dtAcc, healthBuf;
+    DeviceBuffer potential;                 // SelfGravitation::potentialBuffer (V values)
+    GravityConst<real> gc;                  // relaxation / gravity-source constants
+    // the potential the flux kernels see: null while it is zero (its terms change no bit)
+    const real* livePotential() const { return potentialLive_ ? potential.as<real>() : nullptr; }
+    void relaxPotential(const real* densitySource, int sweeps);   // sweeps x (ghost fill, relax)
     std::unique_ptr<Equation> equation;
     std::unique_ptr<Integrator<real>> integrator;
     StepConst<real>* sc() const { return stepConst.as<StepConst<real>>(); }
@@ -218,7 +237,8 @@ protected:
     virtual void calcTimestep() = 0;        // device-side; leaves the minimum in dtAcc
     virtual void step() = 0;
     void finalizeDt(bool fixed);
-    void applyPotential();                  // SelfGravitation::applyPotential with a zero potential
+    void applyPotential();                  // SelfGravitation::applyPotential (SelfGravitation.cpp:100-124)
+    bool potentialLive_ = false;            // useGravity, or a nonzero static potential was given
 };
 
 template <typename real>

@@ -89,6 +89,10 @@ __device__ __forceinline__ void boundaryLine(const Grid& g, int axis, int N, int
     }
 }
 
+template <typename real, int D>
+__device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan<real>& plan,
+                                                const StepConst<real>& sc, long long c, long long off);
+
 // Flux divergence and Runge-Kutta combine of one cell (res/CalcFluxDeriv.cl:7-44 and
 // the multAdd chain).  `off` is the cell offset of this grid inside the slot arrays
 // (0 for a single problem; the problem's first cell in a batch).
@@ -113,6 +117,15 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
 #pragma unroll
         for (int j = 0; j < N; ++j) d[j] = (real)0.;
     }
+    combinePlanCell<real, D>(d, plan, sc, c, off);
+}
+
+// The integrator's use of one cell's deriv d: ForwardEuler's state += deriv * dt, or
+// this stage's column of the Runge-Kutta rows (see combine.cu).
+template <typename real, int D>
+__device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan<real>& plan,
+                                                const StepConst<real>& sc, long long c, long long off) {
+    const int N = D + 2;
     if (plan.fe) {                                            // ForwardEuler::integrate: state += deriv * dt
         real dt = sc.dt;
         real* s = plan.slot[0] + (long long)N * (off + c);

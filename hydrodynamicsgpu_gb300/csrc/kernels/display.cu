@@ -5,8 +5,8 @@
 // display index is the reference's DISPLAY_* enum, whose numbering depends on dim
 // (src/Equation/Euler.cpp:18-27): DENSITY, VELOCITY, VELOCITY_X, [VELOCITY_Y],
 // [VELOCITY_Z], PRESSURE, ENERGY_INTERNAL, ENERGY_KINETIC, ENERGY_TOTAL, POTENTIAL.
-// The gravitational potential is zero on this path (the self-gravity pass with a
-// zero potential), so energyPotential = density * 0.
+// energyPotential = density * potential, with the solver's potential buffer (zero
+// unless self-gravity or a static potential is in use).
 #include "kernels.h"
 
 namespace hgpu {
@@ -16,7 +16,8 @@ constexpr int kThreads = 256;
 
 template <typename real, int D>
 __global__ void __launch_bounds__(kThreads) displayKernel(Grid g, real gamma, int kind,
-                                                          const real* __restrict__ state, float* __restrict__ out) {
+                                                          const real* __restrict__ state, float* __restrict__ out,
+                                                          const real* __restrict__ pot) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
     const int E = D + 1;
@@ -30,7 +31,8 @@ __global__ void __launch_bounds__(kThreads) displayKernel(Grid g, real gamma, in
     for (int k = 1; k < D; ++k) velocitySq = velocitySq + v[k] * v[k];
     const real energyTotal = st[E];
     const real energyKinetic = (real)(.5 * (double)density * (double)velocitySq);   // `.5 * density * velocitySq`
-    const real energyPotential = density * (real)0;
+    const real potential = pot ? pot[c] : (real)0;
+    const real energyPotential = density * potential;
     const real energyInternal = energyTotal - energyKinetic - energyPotential;
     real value = 0;
     switch (kind) {
@@ -43,7 +45,7 @@ __global__ void __launch_bounds__(kThreads) displayKernel(Grid g, real gamma, in
     case 6: value = energyInternal; break;
     case 7: value = energyKinetic; break;
     case 8: value = energyTotal; break;
-    case 9: value = (real)0; break;                                 // gravityPotentialBuffer
+    case 9: value = potential; break;                               // gravityPotentialBuffer
     }
     out[c] = (float)value;
 }
@@ -53,15 +55,16 @@ __global__ void __launch_bounds__(kThreads) displayKernel(Grid g, real gamma, in
 int displayCount(int dim) { return 7 + dim; }
 
 template <typename real>
-void launchDisplay(const Grid& g, real gamma, int method, const real* state, float* out, cudaStream_t st) {
+void launchDisplay(const Grid& g, real gamma, int method, const real* state, float* out, cudaStream_t st,
+                   const real* pot) {
     const int kind = method >= 2 + g.dim ? method + (3 - g.dim) : method;   // the dim-3 numbering
     const unsigned blocks = (unsigned)((g.V + kThreads - 1) / kThreads);
-    if (g.dim == 1) displayKernel<real, 1><<<blocks, kThreads, 0, st>>>(g, gamma, kind, state, out);
-    else if (g.dim == 2) displayKernel<real, 2><<<blocks, kThreads, 0, st>>>(g, gamma, kind, state, out);
-    else displayKernel<real, 3><<<blocks, kThreads, 0, st>>>(g, gamma, kind, state, out);
+    if (g.dim == 1) displayKernel<real, 1><<<blocks, kThreads, 0, st>>>(g, gamma, kind, state, out, pot);
+    else if (g.dim == 2) displayKernel<real, 2><<<blocks, kThreads, 0, st>>>(g, gamma, kind, state, out, pot);
+    else displayKernel<real, 3><<<blocks, kThreads, 0, st>>>(g, gamma, kind, state, out, pot);
 }
 
-template void launchDisplay<double>(const Grid&, double, int, const double*, float*, cudaStream_t);
-template void launchDisplay<float>(const Grid&, float, int, const float*, float*, cudaStream_t);
+template void launchDisplay<double>(const Grid&, double, int, const double*, float*, cudaStream_t, const double*);
+template void launchDisplay<float>(const Grid&, float, int, const float*, float*, cudaStream_t, const float*);
 
 }  // namespace hgpu

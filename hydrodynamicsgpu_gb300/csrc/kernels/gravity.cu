@@ -1,0 +1,194 @@
+// gravity.cu -- self-gravity with a live potential for sm_103a: the potential's
+// starting guess, its ghost fill, the Poisson relaxation sweeps and the gravity
+// source term fused with the integrator's combine.
+//
+// Reference pieces replaced (KennethYeah/HydrodynamicsGPU):
+//  * SelfGravitation::resetState (src/Solver/SelfGravitation.cpp:35-98): with
+//    useGravity the potential starts as -density, is relaxed, and the starting guess
+//    (the host vector, not the relaxed buffer) is added to the total energy;
+//  * SelfGravitation::potentialBoundary (:126-140) with the potential's boundary
+//    kernels (include/HydroGPU/Equation/SelfGravitationBehavior.h:22-34: PERIODIC ->
+//    periodic, MIRROR and FREEFLOW -> free flow) on a stride-1 buffer;
+//  * gravityPotentialPoissonRelax (res/SelfGravitation.cl:20-63).  The reference
+//    kernel updates the potential in place while its neighbours read it, so a launch
+//    has no single result: each order in which a device runs the work-items gives its
+//    own.  Here a launch is the red-black order, one of those the reference permits:
+//    every interior cell with x + y + z even first (their neighbours are all odd, so
+//    these updates do not see each other), then every odd cell (reading the new even
+//    values).  It is deterministic and each half is one parallel sweep;
+//  * calcGravityDeriv (res/SelfGravitation.cl:65-102) into a deriv that goes straight
+//    into the integrator's combine (combinePlanCell), as the flux divergence does.
+// Per-cell expressions follow the reference's operation order and types: in FP32 the
+// double literals of `4. * M_PI * G * density`, `-2. * (1. / (DX * DX) ...)` and
+// `/ (2. * dx[side])` promote those expressions to double.
+#include "../../../include/hgpu/hgpu.h"
+#include "combine_cells.cuh"
+#include "gravity.h"
+
+namespace hgpu {
+namespace {
+
+constexpr int kThreads = 256;
+inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// potential = -density (useGravity) or the given channel; total energy += that potential
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) potentialInitKernel(Grid g, int fromDensity, real* __restrict__ state,
+                                                                real* __restrict__ pot) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    real* s = state + (long long)(D + 2) * c;
+    const real p = fromDensity ? -s[0] : pot[c];
+    pot[c] = p;
+    s[D + 1] = s[D + 1] + p;
+}
+
+// the potential's ghost fill along one axis: boundaryLine on a one-component buffer
+template <typename real>
+__global__ void __launch_bounds__(kThreads) potentialBoundaryKernel(Grid g, int axis, int mMin, int mMax,
+                                                                    real* __restrict__ pot) {
+    boundaryLine<real>(g, axis, 1, mMin, mMax, pot, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// one colour of a relaxation sweep: thread t -> the t-th interior cell of that colour
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) relaxKernel(Grid g, GravityConst<real> gc, int colour,
+                                                        const real* __restrict__ state, real* __restrict__ pot) {
+    // interior extents and the colour's cells per x-row (x from 2 to S0-3)
+    const int nx = g.S[0] - 4, ny = D > 1 ? g.S[1] - 4 : 1, nz = D > 2 ? g.S[2] - 4 : 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int halfRow = (nx + 1) / 2;                        // cells of one colour per row (upper bound)
+    const long long rows = (long long)ny * nz;
+    if (t >= rows * halfRow) return;
+    const int r = (int)(t / halfRow), k = (int)(t % halfRow);
+    const int iy = r % ny, iz = r / ny;
+    const int y = D > 1 ? iy + 2 : 0, z = D > 2 ? iz + 2 : 0;
+    // x = 2 + 2k + shift, with shift chosen so that x + y + z has the colour's parity
+    const int shift = ((2 + y + z) & 1) ^ colour;
+    const int x = 2 + 2 * k + shift;
+    if (x >= g.S[0] - 2) return;
+    const long long c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
+    // skewSum: +x, -x, +y, -y, +z, -z neighbours inside [2, S-3] (SelfGravitation.cl:39-51)
+    real skewSum = (real)0;
+    if (x < g.S[0] - 3) skewSum = skewSum + divI(pot[c + 1], gc.dxSq[0]);
+    if (x > 2) skewSum = skewSum + divI(pot[c - 1], gc.dxSq[0]);
+    if (D > 1) {
+        const long long sy = g.step[1];
+        if (y < g.S[1] - 3) skewSum = skewSum + divI(pot[c + sy], gc.dxSq[1]);
+        if (y > 2) skewSum = skewSum + divI(pot[c - sy], gc.dxSq[1]);
+    }
+    if (D > 2) {
+        const long long sz = g.step[2];
+        if (z < g.S[2] - 3) skewSum = skewSum + divI(pot[c + sz], gc.dxSq[2]);
+        if (z > 2) skewSum = skewSum + divI(pot[c - sz], gc.dxSq[2]);
+    }
+    const real density = state[(long long)(D + 2) * c];
+    // (4. * M_PI * G * density - skewSum) / diag, in double for both precisions
+    pot[c] = (real)divI(mulI(gc.fourPiG, (double)density) - (double)skewSum, gc.diag);
+}
+
+// calcGravityDeriv of one cell into d (zero outside the interior), then the combine
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) gravityCombineKernel(Grid g, GravityConst<real> gc,
+                                                                 const real* __restrict__ stage,
+                                                                 const real* __restrict__ pot, CombinePlan<real> plan,
+                                                                 const StepConst<real>* __restrict__ sc) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    int x, y, z;
+    cellCoords(g, c, x, y, z);
+    const int N = D + 2, E = D + 1;
+    real d[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) d[j] = (real)0;
+    if (inRange(g, x, y, z, 2, 2)) {
+        const real* st = stage + (long long)N * c;
+        const real density = st[0];
+        real derivEnergyTotal = (real)0;
+#pragma unroll
+        for (int side = 0; side < D; ++side) {
+            const long long sp = g.step[side];
+            const real dphi = pot[c + sp] - pot[c - sp];
+            // (phi[next] - phi[prev]) / (2. * dx[side]): a double quotient, stored as real
+            const real gradient = (real)divI((double)dphi, gc.twoDx[side]);
+            const real gravity = -gradient;
+            const real f = mulI(density, gravity);
+            d[1 + side] = zfix(-f);                                  // deriv (+0) -= density * gravity
+            const real e = mulI(f, st[1 + side]);
+            derivEnergyTotal = side == 0 ? zfix(-e) : derivEnergyTotal - e;
+        }
+        d[E] = zfix(derivEnergyTotal);                               // deriv[E] (+0) += derivEnergyTotal
+    }
+    combinePlanCell<real, D>(d, plan, *sc, c, 0);
+}
+
+}  // namespace
+
+template <typename real>
+GravityConst<real> gravityConst(const double dx[3], double G, int dim) {
+    GravityConst<real> gc;
+    // ((real)G) as the program's define makes it; 4. * M_PI * G in double, left to right
+    gc.fourPiG = (4. * 3.14159265358979323846) * (double)(real)G;
+    double invSum = 0.;
+    for (int i = 0; i < dim; ++i) {
+        const real dxr = (real)dx[i];
+        const real sq = dxr * dxr;                                  // DX * DX in the program's type
+        gc.dxSq[i] = sq;
+        invSum = i == 0 ? 1. / (double)sq : invSum + 1. / (double)sq;
+        gc.twoDx[i] = 2. * (double)dxr;
+    }
+    for (int i = dim; i < 3; ++i) { gc.dxSq[i] = (real)1; gc.twoDx[i] = 2.; }
+    gc.diag = (double)(real)(-2. * invSum);                          // `const real diag`
+    return gc;
+}
+
+template <typename real>
+void launchPotentialInit(const Grid& g, int fromDensity, real* state, real* pot, cudaStream_t st) {
+    if (g.dim == 1) potentialInitKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, fromDensity, state, pot);
+    else if (g.dim == 2) potentialInitKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, fromDensity, state, pot);
+    else potentialInitKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, fromDensity, state, pot);
+}
+
+template <typename real>
+void launchPotentialBoundary(const Grid& g, const int methods[3][2], real* pot, cudaStream_t st) {
+    for (int axis = 0; axis < g.dim; ++axis) {
+        int m[2];
+        for (int k = 0; k < 2; ++k)
+            m[k] = methods[axis][k] == HGPU_BOUNDARY_MIRROR ? HGPU_BOUNDARY_FREEFLOW : methods[axis][k];
+        const long long n = g.dim == 1 ? 1 : (long long)g.S[axis == 0 ? 1 : 0] * g.S[axis == 2 ? 1 : 2];
+        potentialBoundaryKernel<real><<<blocksFor(n), kThreads, 0, st>>>(g, axis, m[0], m[1], pot);
+    }
+}
+
+template <typename real>
+void launchRelaxSweep(const Grid& g, const GravityConst<real>& gc, const real* state, real* pot, cudaStream_t st) {
+    const long long nx = g.S[0] - 4, ny = g.dim > 1 ? g.S[1] - 4 : 1, nz = g.dim > 2 ? g.S[2] - 4 : 1;
+    if (nx <= 0 || ny <= 0 || nz <= 0) return;
+    const long long n = ny * nz * ((nx + 1) / 2);
+    for (int colour = 0; colour < 2; ++colour) {
+        if (g.dim == 1) relaxKernel<real, 1><<<blocksFor(n), kThreads, 0, st>>>(g, gc, colour, state, pot);
+        else if (g.dim == 2) relaxKernel<real, 2><<<blocksFor(n), kThreads, 0, st>>>(g, gc, colour, state, pot);
+        else relaxKernel<real, 3><<<blocksFor(n), kThreads, 0, st>>>(g, gc, colour, state, pot);
+    }
+}
+
+template <typename real>
+void launchGravityCombine(const Grid& g, const GravityConst<real>& gc, const real* stage, const real* pot,
+                          const CombinePlan<real>& plan, const StepConst<real>* sc, cudaStream_t st) {
+    if (g.dim == 1) gravityCombineKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, gc, stage, pot, plan, sc);
+    else if (g.dim == 2) gravityCombineKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, gc, stage, pot, plan, sc);
+    else gravityCombineKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, gc, stage, pot, plan, sc);
+}
+
+#define INST(real)                                                                                              \
+    template GravityConst<real> gravityConst<real>(const double[3], double, int);                              \
+    template void launchPotentialInit<real>(const Grid&, int, real*, real*, cudaStream_t);                      \
+    template void launchPotentialBoundary<real>(const Grid&, const int[3][2], real*, cudaStream_t);            \
+    template void launchRelaxSweep<real>(const Grid&, const GravityConst<real>&, const real*, real*, cudaStream_t); \
+    template void launchGravityCombine<real>(const Grid&, const GravityConst<real>&, const real*, const real*,    \
+                                             const CombinePlan<real>&, const StepConst<real>*, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace hgpu

@@ -1,0 +1,33 @@
+// gravity.h -- launchers of the self-gravity kernels (gravity.cu).
+#pragma once
+#include "kernels.h"
+
+namespace hgpu {
+
+// Constants of the relaxation and the gravity source, as the program bakes them.
+template <typename real>
+struct GravityConst {
+    double fourPiG;   // 4. * M_PI * ((real)G), double
+    double diag;      // (double)(real)(-2. * (1. / (DX * DX) + ...)), `const real diag`
+    real dxSq[3];     // DX * DX in the program's type
+    double twoDx[3];  // 2. * dx[side], double
+};
+
+template <typename real>
+GravityConst<real> gravityConst(const double dx[3], double G, int dim);
+
+// potential = -density (fromDensity) or its current contents; total energy += potential
+template <typename real>
+void launchPotentialInit(const Grid& g, int fromDensity, real* state, real* pot, cudaStream_t st);
+// SelfGravitation::potentialBoundary: every axis, min then max side
+template <typename real>
+void launchPotentialBoundary(const Grid& g, const int methods[3][2], real* pot, cudaStream_t st);
+// one gravityPotentialPoissonRelax launch in the red-black order (two kernels)
+template <typename real>
+void launchRelaxSweep(const Grid& g, const GravityConst<real>& gc, const real* state, real* pot, cudaStream_t st);
+// calcGravityDeriv of the stage state, fused with the integrator's combine
+template <typename real>
+void launchGravityCombine(const Grid& g, const GravityConst<real>& gc, const real* stage, const real* pot,
+                          const CombinePlan<real>& plan, const StepConst<real>* sc, cudaStream_t st);
+
+}  // namespace hgpu

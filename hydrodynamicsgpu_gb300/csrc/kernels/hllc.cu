@@ -20,14 +20,15 @@ namespace {
 constexpr int kThreads = 256;
 inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
-template <typename real, int D, bool HLL>
+template <typename real, int D, bool HLL, bool GRAV>
 __global__ void __launch_bounds__(kThreads) hllcWaveKernel(Grid g, Phys<real> ph, double gq,
-                                                           const real* __restrict__ state, real* __restrict__ waves) {
+                                                           const real* __restrict__ state, real* __restrict__ waves,
+                                                           const real* __restrict__ pot) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    hllcWaveCell<real, D, HLL>(g, ph, gq, state, waves, c, x, y, z);
+    hllcWaveCell<real, D, HLL, GRAV>(g, ph, gq, state, waves, c, x, y, z, pot);
 }
 
 template <typename real, int D>
@@ -45,24 +46,27 @@ __global__ void __launch_bounds__(kThreads) hllcDtKernel(Grid g, Phys<real> ph, 
     blockMinToGlobal(best, acc);
 }
 
-template <typename real, int D, bool HLL>
+template <typename real, int D, bool HLL, bool GRAV>
 __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph, const real* __restrict__ stage,
                                                            const real* __restrict__ waves, real* __restrict__ flux,
-                                                           unsigned* health) {
+                                                           unsigned* health, const real* __restrict__ pot) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.V) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
-    if (!hllcFluxCell<real, D, HLL>(g, ph, stage, waves, flux, c, x, y, z)) atomicOr(health, HEALTH_HLLC_NOBRANCH);
+    if (!hllcFluxCell<real, D, HLL, GRAV>(g, ph, stage, waves, flux, c, x, y, z, pot))
+        atomicOr(health, HEALTH_HLLC_NOBRANCH);
 }
 
 }  // namespace
 
-template <typename real>
-void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st) {
+// pot: the gravitational potential, or null for a zero potential
+template <typename real, bool GRAV>
+void launchHllcWavesG(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st,
+                      const real* pot) {
     // (gamma + 1.) / (2. * gamma) is a per-program constant (double literals); computed once, identically
     double gq = ((double)ph.gamma + 1.) / (2. * (double)ph.gamma);
-#define L(DD, H) hllcWaveKernel<real, DD, H><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves)
+#define L(DD, H) hllcWaveKernel<real, DD, H, GRAV><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves, pot)
     if (hll) {
         if (g.dim == 1) L(1, true);
         else if (g.dim == 2) L(2, true);
@@ -73,6 +77,13 @@ void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, rea
         else L(3, false);
     }
 #undef L
+}
+
+template <typename real>
+void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st,
+                     const real* pot) {
+    if (pot) launchHllcWavesG<real, true>(g, ph, state, waves, hll, st, pot);
+    else launchHllcWavesG<real, false>(g, ph, state, waves, hll, st, nullptr);
 }
 
 template <typename real>
@@ -83,10 +94,11 @@ void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsign
     else hllcDtKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, waves, acc, health);
 }
 
-template <typename real>
-void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                    unsigned* health, int hll, cudaStream_t st) {
-#define L(DD, H) hllcFluxKernel<real, DD, H><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health)
+template <typename real, bool GRAV>
+void launchHllcFluxG(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
+                     unsigned* health, int hll, cudaStream_t st, const real* pot) {
+#define L(DD, H) \
+    hllcFluxKernel<real, DD, H, GRAV><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health, pot)
     if (hll) {
         if (g.dim == 1) L(1, true);
         else if (g.dim == 2) L(2, true);
@@ -99,12 +111,20 @@ void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, cons
 #undef L
 }
 
+template <typename real>
+void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
+                    unsigned* health, int hll, cudaStream_t st, const real* pot) {
+    if (pot) launchHllcFluxG<real, true>(g, ph, stage, waves, flux, health, hll, st, pot);
+    else launchHllcFluxG<real, false>(g, ph, stage, waves, flux, health, hll, st, nullptr);
+}
+
 #define INST(real)                                                                                                \
-    template void launchHllcWaves<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t);   \
+    template void launchHllcWaves<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t,    \
+                                        const real*);                                                             \
     template void launchHllcDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                      cudaStream_t);                                                               \
     template void launchHllcFlux<real>(const Grid&, const Phys<real>&, const real*, const real*, real*, unsigned*, \
-                                       int, cudaStream_t);
+                                       int, cudaStream_t, const real*);
 INST(double)
 INST(float)
 #undef INST

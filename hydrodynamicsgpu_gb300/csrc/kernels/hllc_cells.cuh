@@ -15,13 +15,15 @@ __device__ __forceinline__ void loadRotated(const real* __restrict__ s, long lon
 
 template <typename real, int D>
 struct Prim {
-    real density, invDensity, v[3], velocitySq, energyTotal, pressure, enthalpyTotal;
+    real density, invDensity, v[3], velocitySq, energyTotal, pressure, enthalpyTotal, potential;
 };
 
-// primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238), potential 0.
+// primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238).  GRAV: with
+// the cell's potential phi (energyInternal = energyTotal - energyKinetic - phi);
+// otherwise the potential is zero and that term, which would change no bit, is left out.
 // `1. / densityL` and `(gamma - 1.) * ...` use double literals: FP32 promotes them.
-template <typename real, int D>
-__device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real, D>& p) {
+template <typename real, int D, bool GRAV = false>
+__device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real, D>& p, real phi = (real)0) {
     const int E = D + 1;
     p.density = st[0];
     p.invDensity = (real)divI(1., (double)p.density);
@@ -34,21 +36,24 @@ __device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real
     p.energyTotal = mulI(st[E], p.invDensity);
     real energyKinetic = halfOf(p.velocitySq);                          // .5f * velocitySq
     real energyInternal = p.energyTotal - energyKinetic;
+    if (GRAV) energyInternal = energyInternal - phi;
+    p.potential = phi;
     p.pressure = (real)mulI(mulI((double)gamma - 1., (double)p.density), (double)energyInternal);
     p.enthalpyTotal = p.energyTotal + mulI(p.pressure, p.invDensity);
 }
 
 // sl, sr of one face (EulerHLLC.cl:85-97)
-template <typename real, int D, int SIDE>
+template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, double gq, const real* __restrict__ state,
-                                         real* __restrict__ waves, long long c) {
+                                         real* __restrict__ waves, long long c,
+        const real* __restrict__ pot = nullptr) {
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
     const double gm1 = (double)ph.gamma - 1.;
     Prim<real, D> L, R;
-    primitives<real, D>(sL, ph.gamma, L);
-    primitives<real, D>(sR, ph.gamma, R);
+    primitives<real, D, GRAV>(sL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
+    primitives<real, D, GRAV>(sR, ph.gamma, R, GRAV ? pot[c] : (real)0);
     real cL = (real)sqrt(mulI(gm1, (double)(L.enthalpyTotal - halfOf(L.velocitySq))));
     real cR = (real)sqrt(mulI(gm1, (double)(R.enthalpyTotal - halfOf(R.velocitySq))));
     // .5f * (pL + pR) - .5f * (vR - vL) * .5f * (rhoL + rhoR) * .5f * (cL + cR), halvings exact
@@ -67,16 +72,17 @@ __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, do
 // EulerHLL sl, sr of one face (EulerHLL.cl:17-116): Davis direct bounded,
 // sl = min(vL - cL, v - c), sr = max(vR + cR, v + c) with v, c from the Roe averages.
 // `.5 * velocitySq` and `(gamma - 1.)` are double literals there (FP32 promotes).
-template <typename real, int D, int SIDE>
+template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void hllWaveFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ state,
-                                            real* __restrict__ waves, long long c) {
+                                            real* __restrict__ waves, long long c,
+        const real* __restrict__ pot = nullptr) {
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
     const double gm1 = (double)ph.gamma - 1.;
     Prim<real, D> L, R;
-    primitives<real, D>(sL, ph.gamma, L);
-    primitives<real, D>(sR, ph.gamma, R);
+    primitives<real, D, GRAV>(sL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
+    primitives<real, D, GRAV>(sR, ph.gamma, R, GRAV ? pot[c] : (real)0);
     const real cL = (real)sqrt(mulI(gm1, (double)L.enthalpyTotal - halfOf((double)L.velocitySq)));
     const real cR = (real)sqrt(mulI(gm1, (double)R.enthalpyTotal - halfOf((double)R.velocitySq)));
     const real wL = sqrt(L.density), wR = sqrt(R.density);
@@ -88,28 +94,30 @@ __device__ __forceinline__ void hllWaveFace(const Grid& g, const Phys<real>& ph,
     vv = mulI(v[0], v[0]);
 #pragma unroll
     for (int k = 1; k < D; ++k) vv = vv + mulI(v[k], v[k]);
-    // (the Roe-averaged potential energy is +0: subtracting it changes no bit)
-    const real cs = (real)sqrt(mulI(gm1, (double)H - halfOf((double)vv)));
+    // - energyPotential, the Roe average of the potential (zero without GRAV: left out)
+    double hc = (double)H - halfOf((double)vv);
+    if (GRAV) hc = hc - (double)mulI(mulI(wL, L.potential) + mulI(wR, R.potential), norm);
+    const real cs = (real)sqrt(mulI(gm1, hc));
     waves[((long long)SIDE * 2 + 0) * g.V + c] = fminLibm(L.v[0] - cL, v[0] - cs);
     waves[((long long)SIDE * 2 + 1) * g.V + c] = fmaxLibm(R.v[0] + cR, v[0] + cs);
 }
 
 // wave speeds of the faces of one cell: every axis in [2, S-2] (EulerHLLC.cl:110-131)
 // (HLL: EulerHLL's wave speeds instead, EulerHLL.cl:118-138)
-template <typename real, int D, bool HLL = false>
+template <typename real, int D, bool HLL = false, bool GRAV = false>
 __device__ __forceinline__ void hllcWaveCell(const Grid& g, const Phys<real>& ph, double gq,
                                              const real* __restrict__ state, real* __restrict__ waves, long long c,
-                                             int x, int y, int z) {
+                                             int x, int y, int z, const real* __restrict__ pot = nullptr) {
     if (!inRange(g, x, y, z, 2, 1)) return;
     if (HLL) {
-        hllWaveFace<real, D, 0>(g, ph, state, waves, c);
-        if (D > 1) hllWaveFace<real, D, (D > 1 ? 1 : 0)>(g, ph, state, waves, c);
-        if (D > 2) hllWaveFace<real, D, (D > 2 ? 2 : 0)>(g, ph, state, waves, c);
+        hllWaveFace<real, D, 0, GRAV>(g, ph, state, waves, c, pot);
+        if (D > 1) hllWaveFace<real, D, (D > 1 ? 1 : 0), GRAV>(g, ph, state, waves, c, pot);
+        if (D > 2) hllWaveFace<real, D, (D > 2 ? 2 : 0), GRAV>(g, ph, state, waves, c, pot);
         return;
     }
-    waveFace<real, D, 0>(g, ph, gq, state, waves, c);
-    if (D > 1) waveFace<real, D, (D > 1 ? 1 : 0)>(g, ph, gq, state, waves, c);
-    if (D > 2) waveFace<real, D, (D > 2 ? 2 : 0)>(g, ph, gq, state, waves, c);
+    waveFace<real, D, 0, GRAV>(g, ph, gq, state, waves, c, pot);
+    if (D > 1) waveFace<real, D, (D > 1 ? 1 : 0), GRAV>(g, ph, gq, state, waves, c, pot);
+    if (D > 2) waveFace<real, D, (D > 2 ? 2 : 0), GRAV>(g, ph, gq, state, waves, c, pot);
 }
 
 // cell timestep (EulerHLLC.cl:135-168): cells in [2, S-2], min over sides of
@@ -135,16 +143,17 @@ __device__ __forceinline__ unsigned long long hllcDtCell(const Grid& g, const Ph
 }
 
 // HLLC flux, HLLC_METHOD 2 (EulerHLLC.cl:240-418); `flux` holds the face's previous value.
-template <typename real, int D, int SIDE>
+template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
-                                         const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c) {
+                                         const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c,
+        const real* __restrict__ pot = nullptr) {
     const int N = D + 2, E = N - 1;
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
     loadRotated<real, D, SIDE>(stage, c, stR);
     Prim<real, D> L, R;
-    primitives<real, D>(stL, ph.gamma, L);
-    primitives<real, D>(stR, ph.gamma, R);
+    primitives<real, D, GRAV>(stL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
+    primitives<real, D, GRAV>(stR, ph.gamma, R, GRAV ? pot[c] : (real)0);
     real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
     real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
     real fL[N], fR[N], flux[N];
@@ -202,16 +211,17 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
 
 // EulerHLL flux (EulerHLL.cl:185-346): fL, fR, or the two-state HLL flux
 // (sr fL - sl fR + sl sr (uR - uL)) / (sr - sl); `flux` holds the face's previous value.
-template <typename real, int D, int SIDE>
+template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
-                                        const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c) {
+                                        const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c,
+        const real* __restrict__ pot = nullptr) {
     const int N = D + 2, E = N - 1;
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
     loadRotated<real, D, SIDE>(stage, c, stR);
     Prim<real, D> L, R;
-    primitives<real, D>(stL, ph.gamma, L);
-    primitives<real, D>(stR, ph.gamma, R);
+    primitives<real, D, GRAV>(stL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
+    primitives<real, D, GRAV>(stR, ph.gamma, R, GRAV ? pot[c] : (real)0);
     const real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
     const real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
     real fL[N], fR[N], flux[N];
@@ -252,10 +262,10 @@ __device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, con
 // HLLC fluxes of the faces of one cell: along [2, S-2], transverse interior [2, S-3]
 // (the faces calcFluxDeriv reads).  Returns false if a face took no flux branch.
 // (HLL: the EulerHLL flux instead)
-template <typename real, int D, bool HLL = false>
+template <typename real, int D, bool HLL = false, bool GRAV = false>
 __device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
                                              const real* __restrict__ waves, real* __restrict__ flux, long long c,
-                                             int x, int y, int z) {
+                                             int x, int y, int z, const real* __restrict__ pot = nullptr) {
     bool ok = true;
     int cc[3] = {x, y, z};
 #pragma unroll
@@ -267,13 +277,13 @@ __device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph
         }
         if (!in) continue;
         if (HLL) {
-            if (side == 0) ok &= hllFace<real, D, 0>(g, ph, stage, waves, flux, c);
-            else if (side == 1) ok &= hllFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
-            else ok &= hllFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+            if (side == 0) ok &= hllFace<real, D, 0, GRAV>(g, ph, stage, waves, flux, c, pot);
+            else if (side == 1) ok &= hllFace<real, D, (D > 1 ? 1 : 0), GRAV>(g, ph, stage, waves, flux, c, pot);
+            else ok &= hllFace<real, D, (D > 2 ? 2 : 0), GRAV>(g, ph, stage, waves, flux, c, pot);
         } else {
-            if (side == 0) ok &= hllcFace<real, D, 0>(g, ph, stage, waves, flux, c);
-            else if (side == 1) ok &= hllcFace<real, D, (D > 1 ? 1 : 0)>(g, ph, stage, waves, flux, c);
-            else ok &= hllcFace<real, D, (D > 2 ? 2 : 0)>(g, ph, stage, waves, flux, c);
+            if (side == 0) ok &= hllcFace<real, D, 0, GRAV>(g, ph, stage, waves, flux, c, pot);
+            else if (side == 1) ok &= hllcFace<real, D, (D > 1 ? 1 : 0), GRAV>(g, ph, stage, waves, flux, c, pot);
+            else ok &= hllcFace<real, D, (D > 2 ? 2 : 0), GRAV>(g, ph, stage, waves, flux, c, pot);
         }
     }
     return ok;

@@ -52,8 +52,10 @@ template <typename real>
 void launchResetAcc(unsigned long long* acc, unsigned long long accInit, cudaStream_t st);
 
 // ---- roe.cu ----
+// pot: the gravitational potential (V values), or null for a zero potential
 template <typename real>
-void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st);
+void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st,
+                    const real* pot = nullptr);
 template <typename real>
 void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigned long long* acc, unsigned* health,
                  cudaStream_t st);
@@ -66,18 +68,20 @@ int roeRecordSize(int dim);
 
 // ---- hllc.cu ----
 template <typename real>
-void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st);
+void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st,
+                     const real* pot = nullptr);
 template <typename real>
 void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsigned long long* acc, unsigned* health,
                   cudaStream_t st);
 template <typename real>
 void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                    unsigned* health, int hll, cudaStream_t st);
+                    unsigned* health, int hll, cudaStream_t st, const real* pot = nullptr);
 
 // ---- display scalar (display.cu, convertToTex): method = the reference's DISPLAY_* index ----
 int displayCount(int dim);
 template <typename real>
-void launchDisplay(const Grid& g, real gamma, int method, const real* state, float* out, cudaStream_t st);
+void launchDisplay(const Grid& g, real gamma, int method, const real* state, float* out, cudaStream_t st,
+                   const real* pot = nullptr);
 
 // ---- tableaus (combine.cu): alpha/beta in double, order ----
 int tableauOrder(int integrator);

@@ -317,6 +317,10 @@ extern "C" int hgpu_cfl_timestep_noalloc(const hgpu_config* cfg, const void* d_s
         setLastError(e.what());
         return e.status;
     }
+    if (cfg->use_gravity) {              // the timestep would need the solver's potential
+        setLastError("hgpu_cfl_timestep_noalloc: a zero gravitational potential only");
+        return HGPU_ERR_UNSUPPORTED;
+    }
     long long blocks = (rc.grid.V + kThreads - 1) / kThreads;
     if (blocks > kMaxBlocks) {
         setLastError("hgpu_cfl_timestep_noalloc: grid of " + std::to_string(rc.grid.V) +

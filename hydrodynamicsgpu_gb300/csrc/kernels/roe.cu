@@ -31,14 +31,15 @@ template <> struct BasisTile<1> { enum { X = 256, Y = 1, Z = 1 }; };
 template <> struct BasisTile<2> { enum { X = 32, Y = 8, Z = 1 }; };
 template <> struct BasisTile<3> { enum { X = 32, Y = 4, Z = 2 }; };
 
-template <typename real, int D>
+template <typename real, int D, bool GRAV>
 __global__ void __launch_bounds__(256) roeBasisKernel(Grid g, Phys<real> ph, const real* __restrict__ state,
-                                                     real* __restrict__ basis, int loA, int hiA) {
+                                                     real* __restrict__ basis, int loA, int hiA,
+                                                     const real* __restrict__ pot) {
     typedef BasisTile<D> T;
     constexpr int HX = T::X + 1, HY = D > 1 ? T::Y + 1 : 1, HZ = D > 2 ? T::Z + 1 : 1;
     __shared__ RoePrim<real, D> prim[HZ * HY * HX];
-    roeBasisTile<real, D>(g, ph, state, basis, loA, hiA, blockIdx.x * T::X, blockIdx.y * T::Y, blockIdx.z * T::Z,
-                          T::X, T::Y, T::Z, prim);
+    roeBasisTile<real, D, GRAV>(g, ph, state, basis, loA, hiA, blockIdx.x * T::X, blockIdx.y * T::Y,
+                                blockIdx.z * T::Z, T::X, T::Y, T::Z, prim, pot);
 }
 
 template <typename real, int D>
@@ -104,22 +105,31 @@ __global__ void __launch_bounds__(kThreads) roeFluxXformKernel(Grid g, const dou
 
 }  // namespace
 
-// REF: faces along [2, S-2] (res/EulerRoe.cl:27-34, res/Roe.cl:88-95); SEAM: [1, S-1].
-template <typename real>
-void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st) {
-    int loA = seam ? 1 : 2, hiA = seam ? 0 : 1;
+template <typename real, bool GRAV>
+void launchRoeBasisG(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int loA, int hiA,
+                     const real* pot, cudaStream_t st) {
     auto grid = [&](int tx, int ty, int tz) {
         return dim3((unsigned)((g.S[0] + tx - 1) / tx), (unsigned)((g.S[1] + ty - 1) / ty),
                     (unsigned)((g.S[2] + tz - 1) / tz));
     };
     if (g.dim == 1)
-        roeBasisKernel<real, 1><<<grid(BasisTile<1>::X, 1, 1), 256, 0, st>>>(g, ph, state, basis, loA, hiA);
+        roeBasisKernel<real, 1, GRAV><<<grid(BasisTile<1>::X, 1, 1), 256, 0, st>>>(g, ph, state, basis, loA, hiA, pot);
     else if (g.dim == 2)
-        roeBasisKernel<real, 2><<<grid(BasisTile<2>::X, BasisTile<2>::Y, 1), 256, 0, st>>>(g, ph, state, basis, loA,
-                                                                                          hiA);
+        roeBasisKernel<real, 2, GRAV><<<grid(BasisTile<2>::X, BasisTile<2>::Y, 1), 256, 0, st>>>(g, ph, state, basis,
+                                                                                                loA, hiA, pot);
     else
-        roeBasisKernel<real, 3><<<grid(BasisTile<3>::X, BasisTile<3>::Y, BasisTile<3>::Z), 256, 0, st>>>(
-            g, ph, state, basis, loA, hiA);
+        roeBasisKernel<real, 3, GRAV><<<grid(BasisTile<3>::X, BasisTile<3>::Y, BasisTile<3>::Z), 256, 0, st>>>(
+            g, ph, state, basis, loA, hiA, pot);
+}
+
+// REF: faces along [2, S-2] (res/EulerRoe.cl:27-34, res/Roe.cl:88-95); SEAM: [1, S-1].
+// pot: the gravitational potential, or null for a zero potential.
+template <typename real>
+void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st,
+                    const real* pot) {
+    int loA = seam ? 1 : 2, hiA = seam ? 0 : 1;
+    if (pot) launchRoeBasisG<real, true>(g, ph, state, basis, loA, hiA, pot, st);
+    else launchRoeBasisG<real, false>(g, ph, state, basis, loA, hiA, nullptr, st);
 }
 
 template <typename real>
@@ -185,7 +195,8 @@ void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* ba
 }
 
 #define INST(real)                                                                                              \
-    template void launchRoeBasis<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t);  \
+    template void launchRoeBasis<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t,    \
+                                       const real*);                                                            \
     template void launchRoeDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                     cudaStream_t);                                                             \
     template void launchRoeDeltaQ<real>(const Grid&, const real*, const real*, real*, int, cudaStream_t);       \

@@ -47,12 +47,15 @@ __device__ __forceinline__ constexpr int perm(int j) { return j == 1 ? 1 + SIDE 
 template <typename real, int D>
 struct RoePrim {
     real v[3];
-    real h;   // enthalpyTotal
-    real w;   // roeWeight = sqrt(density)
+    real h;     // enthalpyTotal
+    real w;     // roeWeight = sqrt(density)
+    real phi;   // energyPotential = potential of the cell (GRAV only)
 };
 
-template <typename real, int D>
-__device__ __forceinline__ void roePrim(const real* s, real gamma, RoePrim<real, D>& P) {
+// GRAV: a live gravitational potential phi (res/EulerRoe.cl:70-80); without it the
+// potential is zero and its terms, which would change no bit, are left out.
+template <typename real, int D, bool GRAV = false>
+__device__ __forceinline__ void roePrim(const real* s, real gamma, RoePrim<real, D>& P, real phi = (real)0) {
     const int E = D + 1;
     const real gm1 = gamma - (real)1.f;
     real rho = s[0];
@@ -67,14 +70,16 @@ __device__ __forceinline__ void roePrim(const real* s, real gamma, RoePrim<real,
     for (int k = 1; k < D; ++k) vv = vv + mulI(P.v[k], P.v[k]);
     real energyTotal = mulI(s[E], invDensity);
     real energyKinetic = halfOf(vv);                                     // .5f * dot(v, v)
-    real energyInternal = energyTotal - energyKinetic;                   // - potential (0)
+    real energyInternal = energyTotal - energyKinetic;                   // - energyPotential
+    if (GRAV) energyInternal = energyInternal - phi;
+    P.phi = phi;
     real pressure = mulI(mulI(gm1, rho), energyInternal);
     P.h = energyTotal + mulI(pressure, invDensity);
     P.w = sqrt(rho);
 }
 
 // Per-face part (res/EulerRoe.cl:85-226): Roe averages, eigenvalues, R and L.
-template <typename real, int D, int SIDE>
+template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void roeBasisFromPrim(const RoePrim<real, D>& L, const RoePrim<real, D>& R, real gamma,
                                                  real* rec) {
     typedef RoeRec<D> R_;
@@ -88,7 +93,12 @@ __device__ __forceinline__ void roeBasisFromPrim(const RoePrim<real, D>& L, cons
     real velocitySq = mulI(v[0], v[0]);
 #pragma unroll
     for (int k = 1; k < D; ++k) velocitySq = velocitySq + mulI(v[k], v[k]);
-    real c = sqrt(mulI(enthalpyTotal - halfOf(velocitySq), gm1));       // - energyPotential (0)
+    real hc = enthalpyTotal - halfOf(velocitySq);
+    if (GRAV) {                                                          // - energyPotential (Roe average)
+        const real energyPotential = mulI(mulI(L.w, L.phi) + mulI(R.w, R.phi), norm);
+        hc = hc - energyPotential;
+    }
+    real c = sqrt(mulI(hc, gm1));
     // rotate: normal velocity first (res/EulerRoe.cl:101-110)
     real vx = v[SIDE];
     real vt[2] = {0, 0};

@@ -27,12 +27,12 @@ __device__ __forceinline__ void loadState(const real* __restrict__ s, long long 
     for (int j = 0; j < D + 2; ++j) out[j] = s[(long long)(D + 2) * c + j];
 }
 
-template <typename real, int D, int SIDE>
+template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void storeFace(const Grid& g, const RoePrim<real, D>& L, const RoePrim<real, D>& R,
                                           real gamma, real* __restrict__ basis, long long c) {
     const int NB = RoeRec<D>::NB;
     real rec[NB];
-    roeBasisFromPrim<real, D, SIDE>(L, R, gamma, rec);
+    roeBasisFromPrim<real, D, SIDE, GRAV>(L, R, gamma, rec);
 #pragma unroll
     for (int k = 0; k < NB; ++k) basis[((long long)SIDE * NB + k) * g.V + c] = rec[k];
 }
@@ -41,11 +41,12 @@ __device__ __forceinline__ void storeFace(const Grid& g, const RoePrim<real, D>&
 // (res/EulerRoe.cl:261-271).  The per-cell primitives of the tile plus one cell below
 // it on every axis go to shared memory `prim` ((TX+1)(TY+1)(TZ+1) entries for the
 // active axes) once; then each thread builds the faces of its own cell.  All threads
-// of the block must call this (it synchronises).
-template <typename real, int D>
+// of the block must call this (it synchronises).  GRAV: with the potential `pot`.
+template <typename real, int D, bool GRAV = false>
 __device__ __forceinline__ void roeBasisTile(const Grid& g, const Phys<real>& ph, const real* __restrict__ state,
                                              real* __restrict__ basis, int loA, int hiA, int x0, int y0, int z0,
-                                             int TX, int TY, int TZ, RoePrim<real, D>* prim) {
+                                             int TX, int TY, int TZ, RoePrim<real, D>* prim,
+                                             const real* __restrict__ pot = nullptr) {
     const int HX = TX + 1, HY = D > 1 ? TY + 1 : 1, HZ = D > 2 ? TZ + 1 : 1;
     const int ox = 1, oy = D > 1 ? 1 : 0, oz = D > 2 ? 1 : 0;
     for (int i = threadIdx.x; i < HX * HY * HZ; i += blockDim.x) {
@@ -55,7 +56,7 @@ __device__ __forceinline__ void roeBasisTile(const Grid& g, const Phys<real>& ph
             long long c = gx + (long long)g.S[0] * (gy + (long long)g.S[1] * gz);
             real s[D + 2];
             loadState<real, D>(state, c, s);
-            roePrim<real, D>(s, ph.gamma, prim[i]);
+            roePrim<real, D, GRAV>(s, ph.gamma, prim[i], GRAV ? pot[c] : (real)0);
         }
     }
     __syncthreads();
@@ -64,11 +65,12 @@ __device__ __forceinline__ void roeBasisTile(const Grid& g, const Phys<real>& ph
     if (tz < TZ && x < g.S[0] && y < g.S[1] && z < g.S[2]) {
         const long long c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
         const int self = (tz + oz) * HY * HX + (ty + oy) * HX + (tx + ox);
-        if (roeFace(g, 0, x, y, z, loA, hiA)) storeFace<real, D, 0>(g, prim[self - 1], prim[self], ph.gamma, basis, c);
+        if (roeFace(g, 0, x, y, z, loA, hiA))
+            storeFace<real, D, 0, GRAV>(g, prim[self - 1], prim[self], ph.gamma, basis, c);
         if (D > 1 && roeFace(g, 1, x, y, z, loA, hiA))
-            storeFace<real, D, (D > 1 ? 1 : 0)>(g, prim[self - HX], prim[self], ph.gamma, basis, c);
+            storeFace<real, D, (D > 1 ? 1 : 0), GRAV>(g, prim[self - HX], prim[self], ph.gamma, basis, c);
         if (D > 2 && roeFace(g, 2, x, y, z, loA, hiA))
-            storeFace<real, D, (D > 2 ? 2 : 0)>(g, prim[self - HX * HY], prim[self], ph.gamma, basis, c);
+            storeFace<real, D, (D > 2 ? 2 : 0), GRAV>(g, prim[self - HX * HY], prim[self], ph.gamma, basis, c);
     }
     __syncthreads();
 }

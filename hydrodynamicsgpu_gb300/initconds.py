@@ -182,3 +182,24 @@ def smooth_perturbation(size, seed=200, amp=1e-2, modes=4):
         ph = rng.uniform(0, 2 * math.pi)
         f += np.sin(2 * math.pi * (kx * x + ky * y) + ph)
     return amp * f / modes
+
+
+def gravity_blobs(size=(64, 64), xmin=(-.5, -.5, -.5), xmax=(.5, .5, .5), gamma=1.4, nblobs=3, seed=7,
+                  pressure=10.0, dtype=np.float64):
+    """Self-gravity workload: uniform background density 1 plus `nblobs` Gaussian
+    over-densities (seeded centres in the inner half of the domain, amplitudes
+    U(1, 3), widths U(.05, .12) of the box), at rest, uniform pressure.  The
+    pressure is high enough that the internal energy stays positive after the
+    reference's reset adds the potential's starting guess (-density) to the total
+    energy."""
+    dim = len([s for s in size if s > 1])
+    x, y, z = mesh(size, xmin, xmax)
+    rng = np.random.default_rng(seed)
+    rho = np.ones_like(x)
+    for _ in range(nblobs):
+        c = rng.uniform(-.25, .25, 3)
+        a = rng.uniform(1., 3.)
+        w = rng.uniform(.05, .12)
+        r2 = (x - c[0]) ** 2 + (y - c[1]) ** 2 * (dim > 1) + (z - c[2]) ** 2 * (dim > 2)
+        rho = rho + a * np.exp(-r2 / (2 * w * w))
+    return build_state_euler(dim, gamma, rho, 0.0, 0.0, 0.0, pressure, dtype)

@@ -137,7 +137,11 @@ typedef struct hgpu_config {
     int integrator;        /* HGPU_INTEGRATOR_* ("integratorName" key)                    */
     int precision;         /* HGPU_FP64 / HGPU_FP32                                       */
     int compat;            /* HGPU_COMPAT_*                                               */
-    int reserved[8];       /* zero                                                        */
+    /* self-gravity (src/Solver/SelfGravitation.cpp:35-124, res/SelfGravitation.cl) */
+    int use_gravity;       /* "useGravity" (config.lua:65; HydroGPUApp.cpp:77, 207)      */
+    int gauss_seidel_max_iter;   /* "gaussSeidelMaxIter" (config.lua:68; HydroGPUApp.cpp:78, 208) */
+    double gravitational_constant; /* defs.selfGrav_gravitationalConstant (config.lua:74) */
+    int reserved[4];       /* zero                                                        */
 } hgpu_config;
 
 typedef struct hgpu_solver hgpu_solver;  /* opaque handle */
@@ -165,9 +169,24 @@ int hgpu_destroy(hgpu_solver* s);
 int hgpu_get_shape(const hgpu_solver* s, int* dim, int* num_states, size_t* volume);
 
 /* Upload a full state (ghosts included, AoS): replaces Solver::resetState's
- * Converter::toGPU (src/Solver/Solver.cpp:333-337, SelfGravitation.cpp:89-97 with a
- * zero potential).  count = V*N elements of the solver's precision. */
+ * Converter::toGPU (src/Solver/Solver.cpp:333-337) and SelfGravitation::resetState
+ * (SelfGravitation.cpp:35-98) with a zero potential channel.  count = V*N elements
+ * of the solver's precision.  With use_gravity the potential starts as -density,
+ * is relaxed 100 x gauss_seidel_max_iter times (ghost fill, then one relaxation
+ * sweep) and the starting guess is added to the total energy, as the reference does. */
 int hgpu_set_state(hgpu_solver* s, const void* host_state, size_t count);
+
+/* The same with the initial conditions' potential channel (V elements, or NULL for
+ * zero; SelfGravitationBehavior's Converter, include/HydroGPU/Solver/
+ * SelfGravitationBehavior.h:54-96): without use_gravity it is uploaded as the
+ * potential (a static field the step's flux and gravity source then see) and added
+ * to the total energy; with use_gravity it is replaced by -density as above. */
+int hgpu_set_state_potential(hgpu_solver* s, const void* host_state, size_t count, const void* host_potential,
+                             size_t potential_count);
+
+/* Download the gravitational potential (V elements, ghosts included): the potential
+ * half of the Converter's fromGPU (SelfGravitationBehavior.h:84-90). */
+int hgpu_get_potential(hgpu_solver* s, void* host_potential, size_t count);
 
 /* Download the full state: replaces Converter::fromGPU (Solver.cpp:339-342). */
 int hgpu_get_state(hgpu_solver* s, void* host_state, size_t count);

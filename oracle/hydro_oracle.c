@@ -55,7 +55,7 @@ static double baked6(double v) {
     return strtod(buf, NULL);
 }
 
-int oracle_resolve(const hgpu_config* cfg, int* dim_out, double dx[3], double* gamma_out) {
+int oracle_resolve(const hgpu_config* cfg, int* dim_out, double dx[3], double* gamma_out, double* g_out) {
     if (!cfg) return HGPU_ERR_ARG;
     int dim = cfg->dim;
     if (dim == 0) {
@@ -82,10 +82,13 @@ int oracle_resolve(const hgpu_config* cfg, int* dim_out, double dx[3], double* g
         dx[i] = cfg->compat == HGPU_COMPAT_REF ? baked6(d) : d;
         if (i < dim && !(dx[i] > 0)) return HGPU_ERR_CONFIG;
     }
+    if (cfg->gauss_seidel_max_iter < 0) return HGPU_ERR_CONFIG;
     {
         char buf[64];
         snprintf(buf, sizeof buf, "%.14g", cfg->gamma);
         *gamma_out = cfg->compat == HGPU_COMPAT_REF ? strtod(buf, NULL) : cfg->gamma;
+        snprintf(buf, sizeof buf, "%.14g", cfg->gravitational_constant);
+        *g_out = cfg->compat == HGPU_COMPAT_REF ? strtod(buf, NULL) : cfg->gravitational_constant;
     }
     *dim_out = dim;
     return HGPU_OK;
@@ -93,14 +96,14 @@ int oracle_resolve(const hgpu_config* cfg, int* dim_out, double dx[3], double* g
 
 int oracle_create(const hgpu_config* cfg, oracle_handle** out) {
     int dim;
-    double dx[3], gamma;
-    int st = oracle_resolve(cfg, &dim, dx, &gamma);
+    double dx[3], gamma, G;
+    int st = oracle_resolve(cfg, &dim, dx, &gamma, &G);
     if (st) return st;
     if (cfg->compat != HGPU_COMPAT_REF) return HGPU_ERR_UNSUPPORTED;
     oracle_handle* h = (oracle_handle*)calloc(1, sizeof *h);
     h->precision = cfg->precision;
-    if (cfg->precision == HGPU_FP32) h->f = create_f32(cfg, dim, dx, gamma);
-    else h->d = create_f64(cfg, dim, dx, gamma);
+    if (cfg->precision == HGPU_FP32) h->f = create_f32(cfg, dim, dx, gamma, G);
+    else h->d = create_f64(cfg, dim, dx, gamma, G);
     *out = h;
     return HGPU_OK;
 }
@@ -116,10 +119,29 @@ size_t oracle_count(const oracle_handle* h) {
     return h->d ? (size_t)h->d->V * h->d->N : (size_t)h->f->V * h->f->N;
 }
 
-int oracle_set_state(oracle_handle* h, const void* src, size_t count) {
+/* Solver::resetState's upload: the state, then SelfGravitation::resetState with the
+ * initial conditions' potential channel (pot: one value per cell, or NULL = zero). */
+int oracle_set_state_potential(oracle_handle* h, const void* src, size_t count, const void* pot, size_t pcount) {
     if (!h || !src || count != oracle_count(h)) return HGPU_ERR_ARG;
-    if (h->d) memcpy(h->d->state, src, count * sizeof(double));
-    else memcpy(h->f->state, src, count * sizeof(float));
+    if (pot && pcount != (size_t)(h->d ? h->d->V : h->f->V)) return HGPU_ERR_ARG;
+    if (h->d) {
+        memcpy(h->d->state, src, count * sizeof(double));
+        resetPotential_f64(h->d, (const double*)pot);
+    } else {
+        memcpy(h->f->state, src, count * sizeof(float));
+        resetPotential_f32(h->f, (const float*)pot);
+    }
+    return HGPU_OK;
+}
+
+int oracle_set_state(oracle_handle* h, const void* src, size_t count) {
+    return oracle_set_state_potential(h, src, count, NULL, 0);
+}
+
+int oracle_get_potential(oracle_handle* h, void* dst, size_t count) {
+    if (!h || !dst || count != (size_t)(h->d ? h->d->V : h->f->V)) return HGPU_ERR_ARG;
+    if (h->d) memcpy(dst, h->d->potential, count * sizeof(double));
+    else memcpy(dst, h->f->potential, count * sizeof(float));
     return HGPU_OK;
 }
 

@@ -35,11 +35,12 @@ typedef struct {
     long V;
     REAL dx[3];        /* DX/DY/DZ as baked into the program (Solver.cpp:272-274) */
     REAL gamma;        /* ((real)<defs value>) (Solver.cpp:298)                  */
+    REAL G;            /* selfGrav_gravitationalConstant = ((real)<defs value>)  */
     float cfl;
     int isHLLC;        /* an HLL-family solver (EulerHLLC or EulerHLL): HLL.cpp driver */
     int isHLL;         /* EulerHLL: Davis-bounded wave speeds, two-state HLL flux     */
     REAL* state;       /* Solver::stateBuffer                                     */
-    REAL* potential;   /* SelfGravitation::potentialBuffer (zero: useGravity=false) */
+    REAL* potential;   /* SelfGravitation::potentialBuffer                        */
     REAL* eigenvalues; /* Roe: V*dim*N; HLL: V*dim*N                               */
     REAL* eigenvectors;/* Roe: V*dim*2*N*N (first N*N = left/inverse, then right) */
     REAL* deltaQTilde; /* Roe: V*dim*N                                            */
@@ -717,7 +718,85 @@ static void FN(calcFluxDeriv)(FN(osolver) * s, REAL* deriv) {
     }
 }
 
-/* ---------------- calcGravityDeriv (SelfGravitation.cl:65-102) with a zero potential ---------------- */
+/* ---------------- self-gravity: SelfGravitation.cpp:35-140, SelfGravitation.cl:20-102 ---------------- */
+
+/* potentialBoundary (SelfGravitation.cpp:126-140): each axis, min then max, with the
+ * potential's kernel for the method (SelfGravitationBehavior.h:22-34: PERIODIC ->
+ * periodic, MIRROR and FREEFLOW -> free flow) on the stride-1 potential buffer */
+static void FN(potentialBoundary)(FN(osolver) * s) {
+    for (int i = 0; i < s->dim; ++i)
+        for (int mm = 0; mm < 2; ++mm) {
+            int method = s->cfg.boundary[i][mm];
+            if (method == HGPU_BOUNDARY_NONE) continue;
+            FN(boundaryKernel)(s, s->potential, 1, 0, method == HGPU_BOUNDARY_PERIODIC ? BK_PERIODIC : BK_FREEFLOW,
+                               i, mm);
+        }
+}
+
+/* gravityPotentialPoissonRelax (SelfGravitation.cl:20-63) at one interior cell */
+static void FN(poissonRelaxCell)(FN(osolver) * s, int x, int y, int z) {
+    const int D = s->dim;
+    REAL* phi = s->potential;
+    long index = IDX(s, x, y, z);
+    REAL skewSum = 0.;
+    if (x < s->S[0] - 3) skewSum += phi[index + s->step[0]] / (s->dx[0] * s->dx[0]);
+    if (x > 2) skewSum += phi[index - s->step[0]] / (s->dx[0] * s->dx[0]);
+    if (D > 1) {
+        if (y < s->S[1] - 3) skewSum += phi[index + s->step[1]] / (s->dx[1] * s->dx[1]);
+        if (y > 2) skewSum += phi[index - s->step[1]] / (s->dx[1] * s->dx[1]);
+    }
+    if (D > 2) {
+        if (z < s->S[2] - 3) skewSum += phi[index + s->step[2]] / (s->dx[2] * s->dx[2]);
+        if (z > 2) skewSum += phi[index - s->step[2]] / (s->dx[2] * s->dx[2]);
+    }
+    REAL diag;
+    if (D == 1) diag = -2. * (1. / (s->dx[0] * s->dx[0]));
+    else if (D == 2) diag = -2. * (1. / (s->dx[0] * s->dx[0]) + 1. / (s->dx[1] * s->dx[1]));
+    else diag = -2. * (1. / (s->dx[0] * s->dx[0]) + 1. / (s->dx[1] * s->dx[1]) + 1. / (s->dx[2] * s->dx[2]));
+    const REAL G = s->G;
+    REAL density = s->state[s->N * index];
+    phi[index] = (4. * M_PI * G * density - skewSum) / diag;
+}
+
+/* One relaxation launch.  The reference kernel writes the potential in place while
+ * other work-items read it, so its result depends on the order the device runs the
+ * work-items in; this restates the red-black order: every interior cell with
+ * x + y + z even, then every odd one (cells of one parity never read each other). */
+static void FN(poissonRelax)(FN(osolver) * s) {
+    for (int colour = 0; colour < 2; ++colour) {
+        FOR_CELLS(s) {
+            if (((x + y + z) & 1) != colour) continue;
+            if (!FN(inRange)(s, x, y, z, 2, 2)) continue;
+            FN(poissonRelaxCell)(s, x, y, z);
+        }
+    }
+}
+
+/* sweeps x (potentialBoundary, relax): SelfGravitation.cpp:81-86 and :112-117 */
+static void FN(relaxPotential)(FN(osolver) * s, int sweeps) {
+    for (int i = 0; i < sweeps; ++i) {
+        FN(potentialBoundary)(s);
+        FN(poissonRelax)(s);
+    }
+}
+
+/* SelfGravitation::resetState (SelfGravitation.cpp:35-98) after the state upload:
+ * potentialVec = -density with useGravity, else the initial conditions' channel (pot,
+ * NULL = zero); upload it; relax 100 x gaussSeidelMaxIter times with useGravity; add
+ * potentialVec (the host vector, not the relaxed buffer) to the total energy. */
+static void FN(resetPotential)(FN(osolver) * s, const REAL* pot) {
+    const int N = s->N, E = N - 1;
+    REAL* vec = (REAL*)calloc((size_t)s->V, sizeof(REAL));
+    for (long i = 0; i < s->V; ++i)
+        vec[i] = s->cfg.use_gravity ? -s->state[N * i] : (pot ? pot[i] : (REAL)0);
+    memcpy(s->potential, vec, sizeof(REAL) * (size_t)s->V);
+    if (s->cfg.use_gravity)
+        for (int tries = 0; tries < 100; ++tries) FN(relaxPotential)(s, s->cfg.gauss_seidel_max_iter);
+    for (long i = 0; i < s->V; ++i) s->state[E + N * i] += vec[i];
+    free(vec);
+}
+
+/* ---------------- calcGravityDeriv (SelfGravitation.cl:65-102) ---------------- */
 static void FN(calcGravityDeriv)(FN(osolver) * s, REAL* deriv) {
     const int N = s->N, D = s->dim, E = N - 1;
     FOR_CELLS(s) {
@@ -756,6 +835,7 @@ static void FN(callback)(FN(osolver) * s, int kind, REAL* deriv, REAL dt) {
         }
         FN(calcFluxDeriv)(s, deriv);
     } else {                           /* SelfGravitation::applyPotential (SelfGravitation.cpp:100-124) */
+        if (s->cfg.use_gravity) FN(relaxPotential)(s, s->cfg.gauss_seidel_max_iter);
         FN(calcGravityDeriv)(s, deriv);
         FN(boundary)(s);
     }
@@ -838,7 +918,8 @@ static void FN(destroy)(FN(osolver) * s) {
     free(s);
 }
 
-static FN(osolver) * FN(create)(const hgpu_config* cfg, int dim, const double dxBaked[3], double gammaBaked) {
+static FN(osolver) * FN(create)(const hgpu_config* cfg, int dim, const double dxBaked[3], double gammaBaked,
+                               double gBaked) {
     FN(osolver)* s = (FN(osolver)*)calloc(1, sizeof(FN(osolver)));
     s->cfg = *cfg;
     s->dim = dim;
@@ -847,6 +928,7 @@ static FN(osolver) * FN(create)(const hgpu_config* cfg, int dim, const double dx
     s->step[0] = 1; s->step[1] = s->S[0]; s->step[2] = s->S[0] * s->S[1];
     s->V = (long)s->S[0] * s->S[1] * s->S[2];
     s->gamma = (REAL)gammaBaked;
+    s->G = (REAL)gBaked;
     s->cfl = cfg->cfl;
     s->isHLLC = cfg->solver == HGPU_SOLVER_HLLC || cfg->solver == HGPU_SOLVER_HLL;
     s->isHLL = cfg->solver == HGPU_SOLVER_HLL;

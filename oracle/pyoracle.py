@@ -52,10 +52,13 @@ def lib():
         L = ctypes.CDLL(LIB_ORACLE)
         P = ctypes.POINTER(_abi.HgpuConfig)
         L.oracle_resolve.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
-                                     ctypes.POINTER(ctypes.c_double)]
+                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.oracle_create.argtypes = [P, ctypes.POINTER(ctypes.c_void_p)]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
         L.oracle_set_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        L.oracle_set_state_potential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                 ctypes.c_void_p, ctypes.c_size_t]
+        L.oracle_get_potential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.oracle_get_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.oracle_update.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_int)]
@@ -68,14 +71,15 @@ def lib():
 
 
 def resolve(cfg):
-    """(dim, baked dx[3], baked gamma) exactly as the reference program preamble bakes them."""
+    """(dim, baked dx[3], baked gamma, baked G) exactly as the reference program preamble bakes them."""
     d = ctypes.c_int()
     dx = (ctypes.c_double * 3)()
     g = ctypes.c_double()
-    st = lib().oracle_resolve(ctypes.byref(cfg), ctypes.byref(d), dx, ctypes.byref(g))
+    G = ctypes.c_double()
+    st = lib().oracle_resolve(ctypes.byref(cfg), ctypes.byref(d), dx, ctypes.byref(g), ctypes.byref(G))
     if st:
         raise ValueError("invalid config: %s" % _abi.STATUS_NAMES.get(st, st))
-    return d.value, [dx[0], dx[1], dx[2]], g.value
+    return d.value, [dx[0], dx[1], dx[2]], g.value, G.value
 
 
 def set_threads(n):
@@ -106,7 +110,7 @@ class Oracle(_Base):
 
     def __init__(self, cfg):
         self.cfg = cfg
-        self.dim, self.dx, self.gamma = resolve(cfg)
+        self.dim, self.dx, self.gamma, self.G = resolve(cfg)
         h = ctypes.c_void_p()
         st = lib().oracle_create(ctypes.byref(cfg), ctypes.byref(h))
         if st:
@@ -120,11 +124,20 @@ class Oracle(_Base):
             lib().oracle_destroy(self.h)
             self.h = None
 
-    def set_state(self, a):
+    def set_state(self, a, potential=None):
         a = np.ascontiguousarray(a, dtype=self._np()).reshape(-1)
         assert a.size == self.count
-        st = lib().oracle_set_state(self.h, a.ctypes.data, a.size)
+        if potential is None:
+            st = lib().oracle_set_state(self.h, a.ctypes.data, a.size)
+        else:
+            p = np.ascontiguousarray(potential, dtype=self._np()).reshape(-1)
+            st = lib().oracle_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size)
         assert st == 0
+
+    def get_potential(self):
+        a = np.empty(_abi.config_volume(self.cfg), dtype=self._np())
+        assert lib().oracle_get_potential(self.h, a.ctypes.data, a.size) == 0
+        return a
 
     def get_state(self):
         a = np.empty(self.count, dtype=self._np())
@@ -171,7 +184,10 @@ def _refcl_lib(path):
     if path not in _refcl_libs:
         L = ctypes.CDLL(path)
         L.refcl_create.argtypes = [ctypes.POINTER(_abi.HgpuConfig), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
-                                   ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]
+                                   ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]
+        L.refcl_set_state_potential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                ctypes.c_void_p, ctypes.c_size_t]
+        L.refcl_get_potential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.refcl_destroy.argtypes = [ctypes.c_void_p]
         L.refcl_set_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.refcl_get_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
@@ -197,14 +213,14 @@ class Refcl(_Base):
 
     def __init__(self, cfg):
         self.cfg = cfg
-        self.dim, self.dx, self.gamma = resolve(cfg)
+        self.dim, self.dx, self.gamma, self.G = resolve(cfg)
         path = _refcl_path(cfg)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         self.L = _refcl_lib(path)
         dx = (ctypes.c_double * 3)(*self.dx)
         h = ctypes.c_void_p()
-        st = self.L.refcl_create(ctypes.byref(cfg), self.dim, dx, self.gamma, ctypes.byref(h))
+        st = self.L.refcl_create(ctypes.byref(cfg), self.dim, dx, self.gamma, self.G, ctypes.byref(h))
         if st:
             raise ValueError("refcl_create: %d" % st)
         self.h = h
@@ -215,9 +231,18 @@ class Refcl(_Base):
             self.L.refcl_destroy(self.h)
             self.h = None
 
-    def set_state(self, a):
+    def set_state(self, a, potential=None):
         a = np.ascontiguousarray(a, dtype=self._np()).reshape(-1)
-        assert self.L.refcl_set_state(self.h, a.ctypes.data, a.size) == 0
+        if potential is None:
+            assert self.L.refcl_set_state(self.h, a.ctypes.data, a.size) == 0
+        else:
+            p = np.ascontiguousarray(potential, dtype=self._np()).reshape(-1)
+            assert self.L.refcl_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size) == 0
+
+    def get_potential(self):
+        a = np.empty(_abi.config_volume(self.cfg), dtype=self._np())
+        assert self.L.refcl_get_potential(self.h, a.ctypes.data, a.size) == 0
+        return a
 
     def get_state(self):
         a = np.empty(self.count, dtype=self._np())

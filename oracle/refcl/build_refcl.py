@@ -118,7 +118,7 @@ def program_source(solver, dim, prec, const_inits):
     lines += [
         "static int g_SIZE_X, g_SIZE_Y, g_SIZE_Z, g_STEP_X, g_STEP_Y, g_STEP_Z, g_STEP_W;",
         "static real g_DX, g_DY, g_DZ;",
-        "static double g_gamma;",
+        "static double g_gamma, g_G;",
         "static int g_limiter;",
         "#define DIM %d" % dim,
         "#define SIZE_X g_SIZE_X", "#define SIZE_Y g_SIZE_Y", "#define SIZE_Z g_SIZE_Z",
@@ -126,7 +126,7 @@ def program_source(solver, dim, prec, const_inits):
         "#define DX g_DX", "#define DY g_DY", "#define DZ g_DZ",
         "#define NUM_STATES %d" % n, "#define NUM_FLUX_STATES %d" % n,
         "#define idealGas_heatCapacityRatio ((real)g_gamma)",
-        "#define selfGrav_gravitationalConstant ((real)1)",
+        "#define selfGrav_gravitationalConstant ((real)g_G)",
     ]
     states = ["DENSITY", "MOMENTUM_X"] + (["MOMENTUM_Y"] if dim > 1 else []) + (["MOMENTUM_Z"] if dim > 2 else []) + ["ENERGY_TOTAL"]
     lines.append("enum {\n" + "".join("\tSTATE_%s,\n" % s for s in states) + "\tNUM_STATE\n};")

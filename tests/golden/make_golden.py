@@ -79,6 +79,29 @@ CASES = [
          cfg=dict(solver="EulerRoe", size=(32, 32), boundary="PERIODIC", limiter="MinMod", integrator="RungeKutta4",
                   cfl=.5, precision=_abi.FP32),
          init=lambda: ic.kelvin_helmholtz(size=(32, 32), seed=0, dtype=np.float32)),
+    # self-gravity (useGravity): Poisson relaxation at reset and in every callback
+    dict(name="blobs_roe_rk2_gravity_periodic_2d", steps=3,
+         cfg=dict(solver="EulerRoe", size=(24, 24), boundary="PERIODIC", limiter="MinMod", integrator="RungeKutta2",
+                  use_gravity=True, gauss_seidel_max_iter=5, gravitational_constant=1.),
+         init=lambda: ic.gravity_blobs(size=(24, 24), seed=7)),
+    dict(name="blobs_roe_rk2_gravity_periodic_2d_fp32", steps=3,
+         cfg=dict(solver="EulerRoe", size=(24, 24), boundary="PERIODIC", limiter="MinMod", integrator="RungeKutta2",
+                  use_gravity=True, gauss_seidel_max_iter=5, gravitational_constant=1., precision=_abi.FP32),
+         init=lambda: ic.gravity_blobs(size=(24, 24), seed=7, dtype=np.float32)),
+    dict(name="blobs_hllc_fe_gravity_freeflow_1d", steps=5,
+         cfg=dict(solver="EulerHLLC", size=(48,), boundary="FREEFLOW", integrator="ForwardEuler",
+                  use_gravity=True, gauss_seidel_max_iter=10, gravitational_constant=.5),
+         init=lambda: ic.gravity_blobs(size=(48,), seed=8)),
+    dict(name="blobs_hll_rk4_gravity_mirror_3d", steps=2,
+         cfg=dict(solver="EulerHLL", size=(10, 10, 10), boundary="MIRROR", integrator="RungeKutta4",
+                  use_gravity=True, gauss_seidel_max_iter=2, gravitational_constant=1.),
+         init=lambda: ic.gravity_blobs(size=(10, 10, 10), seed=9)),
+    # a static potential channel without useGravity (the initial conditions' potential)
+    dict(name="static_potential_roe_rk3tvd_freeflow_2d", steps=3,
+         cfg=dict(solver="EulerRoe", size=(20, 20), boundary="FREEFLOW", limiter="Superbee",
+                  integrator="RungeKutta3TVD"),
+         init=lambda: ic.gravity_blobs(size=(20, 20), seed=10),
+         potential=lambda: ic.smooth_perturbation((20, 20), seed=11, amp=.5).reshape(-1)),
 ]
 
 
@@ -97,16 +120,23 @@ def main():
     for case in CASES:
         cfg = cfg_of(case)
         init = np.ascontiguousarray(case["init"]()).reshape(-1)
+        dtype = init.dtype
+        pot = case["potential"]().astype(dtype) if "potential" in case else None
         r = pyoracle.Refcl(cfg)
-        r.set_state(init)
+        r.set_state(init, pot)
         dts = []
         for _ in range(case["steps"]):
             dts.append(r.update(1))
         out = r.get_state()
         meta = dict(case["cfg"])
         meta["steps"] = case["steps"]
+        extra = {}
+        if pot is not None:
+            extra["potential"] = pot
+        if pot is not None or case["cfg"].get("use_gravity"):
+            extra["final_potential"] = r.get_potential()
         np.savez_compressed(fixture_path(case["name"]), init=init, final=out, dts=np.array(dts),
-                            meta=json.dumps(meta))
+                            meta=json.dumps(meta), **extra)
         with open(fixture_path(case["name"]), "rb") as f:
             manifest[case["name"]] = hashlib.sha256(f.read()).hexdigest()
         print(case["name"], "dt[-1]=%r" % dts[-1])

@@ -46,11 +46,27 @@ def test_config_default_and_status_strings(hg):
         assert hg.lib().hgpu_status_string(code).decode() == name
 
 
-def test_struct_layout_matches_header():
-    import ctypes
+def test_struct_layout_matches_header(tmp_path):
     # offsets as laid out by a C compiler for include/hgpu/hgpu.h (x86-64 and aarch64 agree)
     assert ctypes.sizeof(_abi.HgpuConfig) == 168
-    assert _abi.HgpuConfig.boundary.offset == 96 and _abi.HgpuConfig.reserved.offset == 136
+    assert _abi.HgpuConfig.boundary.offset == 96 and _abi.HgpuConfig.use_gravity.offset == 136
+    assert _abi.HgpuConfig.gravitational_constant.offset == 144 and _abi.HgpuConfig.reserved.offset == 152
+    # and every field against the C compiler itself
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in _abi.HgpuConfig._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "hgpu/hgpu.h"\nint main(void) {\n'
+                   + "".join('printf("%%zu\\n", offsetof(hgpu_config, %s));\n' % n for n in names)
+                   + 'printf("%zu\\n", sizeof(hgpu_config));\nreturn 0;\n}\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = [getattr(_abi.HgpuConfig, n).offset for n in names] + [ctypes.sizeof(_abi.HgpuConfig)]
+    assert got == want
 
 
 def test_null_arguments_rejected(hg):
@@ -91,3 +107,26 @@ def test_batch_rejects_mixed_configs(hg):
     h = ctypes.c_void_p()
     assert hg.lib().hgpu_batch_create(arr, 1, ctypes.byref(h)) == codes["HGPU_ERR_UNSUPPORTED"]
     assert hg.lib().hgpu_batch_create(arr, 0, ctypes.byref(h)) == codes["HGPU_ERR_ARG"]
+
+
+def test_gravity_combinations_refused(hg):
+    """Self-gravity runs on the single-problem REF path; the batch, the SEAM scheme and
+    the allocation-free timestep refuse it before any device work."""
+    codes = {v: k for k, v in _abi.STATUS_NAMES.items()}
+    grav = _abi.make_config(solver="EulerRoe", size=(20, 20), use_gravity=True)
+    arr = (_abi.HgpuConfig * 1)(grav)
+    h = ctypes.c_void_p()
+    assert hg.lib().hgpu_batch_create(arr, 1, ctypes.byref(h)) == codes["HGPU_ERR_UNSUPPORTED"]
+    seam = _abi.make_config(solver="EulerRoe", size=(20, 20), use_gravity=True, compat=_abi.COMPAT_SEAM)
+    assert hg.lib().hgpu_create(ctypes.byref(seam), ctypes.byref(h)) == codes["HGPU_ERR_UNSUPPORTED"]
+    dt = ctypes.c_double()
+    assert hg.lib().hgpu_cfl_timestep_noalloc(ctypes.byref(grav), ctypes.c_void_p(1), ctypes.byref(dt),
+                                              None) == codes["HGPU_ERR_UNSUPPORTED"]
+    bad = _abi.make_config(solver="EulerRoe", size=(20, 20), use_gravity=True, gauss_seidel_max_iter=-1)
+    assert hg.lib().hgpu_create(ctypes.byref(bad), ctypes.byref(h)) == codes["HGPU_ERR_CONFIG"]
+
+
+def test_config_default_gravity_keys(hg):
+    cfg = _abi.HgpuConfig()
+    assert hg.lib().hgpu_config_default(cfg) == 0
+    assert cfg.use_gravity == 0 and cfg.gauss_seidel_max_iter == 20 and cfg.gravitational_constant == 1.

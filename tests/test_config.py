@@ -9,7 +9,7 @@ from hydrodynamicsgpu_gb300 import initconds as ic
 def test_dx_baked_to_six_significant_digits(oracle_mod):
     # toNumericString<double> (include/HydroGPU/toNumericString.h:12-22)
     cfg = _abi.make_config(size=(2048, 2048))
-    dim, dx, gamma = oracle_mod.resolve(cfg)
+    dim, dx, gamma, _ = oracle_mod.resolve(cfg)
     assert dim == 2 and dx[0] == 0.000488281 and dx[1] == 0.000488281
     cfg = _abi.make_config(size=(1024,), xmin=(0.,), xmax=(1.,))
     assert oracle_mod.resolve(cfg)[1][0] == 0.000976562
@@ -26,7 +26,7 @@ def test_gamma_baked_like_lua_numbers(oracle_mod):
 
 def test_seam_mode_keeps_exact_constants(oracle_mod):
     cfg = _abi.make_config(size=(2048, 2048), compat=_abi.COMPAT_SEAM, gamma=5. / 3.)
-    dim, dx, gamma = oracle_mod.resolve(cfg)
+    dim, dx, gamma, _ = oracle_mod.resolve(cfg)
     assert dx[0] == 1.0 / 2048 and gamma == 5. / 3.
 
 

@@ -68,7 +68,7 @@ def gpu_frozen(hg, cfg, u, dts):
 
 def torch_vjp(oracle_mod, cfg, u, lam, dts):
     dim = _abi.config_dim(cfg)
-    _, dx, gamma = oracle_mod.resolve(cfg)
+    _, dx, gamma, _ = oracle_mod.resolve(cfg)
     lim = _abi.LIMITERS[cfg.limiter]
     integ = _abi.INTEGRATORS[cfg.integrator]
     x = torch.tensor(u.reshape(grid_shape(cfg)), requires_grad=True)

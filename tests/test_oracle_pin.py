@@ -85,3 +85,83 @@ def test_pin_display(refcl, solver, dim, prec):
     r.update(1)
     for m in range(len(_abi.display_names(dim))):
         assert np.array_equal(o.display(m), r.display(m), equal_nan=True), m
+
+
+# ---------------- self-gravity (useGravity) and the static potential channel ----------------
+def pin_gravity(mod, cfg, init, steps, potential=None):
+    o = mod.Oracle(cfg)
+    r = mod.Refcl(cfg)
+    o.set_state(init, potential)
+    r.set_state(init, potential)
+    assert same(o.get_state(), r.get_state()), "after reset"
+    assert same(o.get_potential(), r.get_potential()), "potential after reset"
+    for k in range(steps):
+        do, dr = o.update(1), r.update(1)
+        assert do == dr, "step %d dt %r vs %r" % (k, do, dr)
+        a, b = o.get_state(), r.get_state()
+        assert same(a, b), "step %d: %s" % (k, describe_diff(a, b))
+        assert same(o.get_potential(), r.get_potential()), "step %d potential" % k
+
+
+GRAVITY_CASES = list(itertools.product(["EulerRoe", "EulerHLLC", "EulerHLL"], [1, 2, 3],
+                                       ["ForwardEuler", "RungeKutta2Heun", "RungeKutta4", "RungeKutta3TVD"], [0, 1]))
+
+
+@pytest.mark.parametrize("solver,dim,integ,prec", GRAVITY_CASES[::2])
+def test_pin_gravity(refcl, solver, dim, integ, prec):
+    """useGravity: -density start, 100 x maxIter relaxations at reset, maxIter per
+    callback, calcGravityDeriv; mixed boundaries (MIRROR's potential ghosts are free flow)."""
+    from hydrodynamicsgpu_gb300 import initconds as ic
+    size = SMALL[dim]
+    cfg = _abi.make_config(solver=solver, size=size, integrator=integ, precision=prec, use_gravity=True,
+                           gauss_seidel_max_iter=3, gravitational_constant=.7,
+                           boundary=[("PERIODIC", "PERIODIC"), ("MIRROR", "FREEFLOW"), ("FREEFLOW", "MIRROR")])
+    init = ic.gravity_blobs(size=size, seed=dim + 10 * prec, dtype=np.float32 if prec else np.float64)
+    pin_gravity(refcl, cfg, init, steps=2)
+
+
+@pytest.mark.parametrize("solver", ["EulerRoe", "EulerHLLC", "EulerHLL"])
+def test_pin_static_potential(refcl, solver):
+    """No useGravity, a nonzero potential channel: the flux kernels and the source
+    term see it, and the reset adds it to the total energy."""
+    cfg = _abi.make_config(solver=solver, size=SMALL[2], integrator="RungeKutta2", boundary="FREEFLOW")
+    init = random_state(cfg, seed=4, blocky=False)
+    pot = np.random.default_rng(5).uniform(-.2, .2, _abi.config_volume(cfg))
+    pin_gravity(refcl, cfg, init, steps=3, potential=pot)
+
+
+def test_relaxation_fixed_point_is_order_independent(oracle_mod):
+    """The reference's relaxation launch is an in-place update whose result depends on
+    the order of its work-items; the oracle and the GPU use the red-black order.  Every
+    order converges to the same discrete Poisson solution: run to convergence, the
+    red-black result equals a plain lexicographic Gauss-Seidel (the order a sequential
+    device runs) to round-off."""
+    from hydrodynamicsgpu_gb300 import initconds as ic
+    size = (14, 12)
+    cfg = _abi.make_config(solver="EulerRoe", size=size, use_gravity=True, gauss_seidel_max_iter=40,
+                           gravitational_constant=1., boundary="FREEFLOW")
+    init = ic.gravity_blobs(size=size, seed=3)
+    o = oracle_mod.Oracle(cfg)
+    o.set_state(init)
+    red_black = o.get_potential().reshape(size[1], size[0])
+    # lexicographic Gauss-Seidel of gravityPotentialPoissonRelax (res/SelfGravitation.cl:20-63)
+    _, dx, _, G = oracle_mod.resolve(cfg)
+    rho = init.reshape(size[1], size[0], -1)[..., 0]
+    phi = -rho.copy()
+    diag = -2. * (1. / (dx[0] * dx[0]) + 1. / (dx[1] * dx[1]))
+    for _ in range(4000):
+        for y in range(2, size[1] - 2):
+            for x in range(2, size[0] - 2):
+                s = 0.
+                if x < size[0] - 3:
+                    s += phi[y, x + 1] / (dx[0] * dx[0])
+                if x > 2:
+                    s += phi[y, x - 1] / (dx[0] * dx[0])
+                if y < size[1] - 3:
+                    s += phi[y + 1, x] / (dx[1] * dx[1])
+                if y > 2:
+                    s += phi[y - 1, x] / (dx[1] * dx[1])
+                phi[y, x] = (4. * np.pi * G * rho[y, x] - s) / diag
+    inner = (slice(2, size[1] - 2), slice(2, size[0] - 2))
+    err = np.abs(red_black[inner] - phi[inner]).max() / np.abs(phi[inner]).max()
+    assert err < 1e-12, err

@@ -39,7 +39,7 @@ def test_torch_step_matches_oracle(oracle_mod, dim, bnd, integ, lim):
     o.set_state(u)
     dt = o.update(1)
     ref = o.get_state()
-    _, dx, gamma = oracle_mod.resolve(cfg)
+    _, dx, gamma, _ = oracle_mod.resolve(cfg)
     out = te.step(torch.tensor(u.reshape(grid_shape(cfg))), dim, dx, gamma, dt, lim, integ, methods_of(cfg, dim))
     out = out.reshape(-1).numpy()
     assert np.all(np.isfinite(ref))
