@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batched sweep")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
+    ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity measurement")
+    ap.add_argument("--gravity-size", type=int, default=2048)
     ap.add_argument("--batch-problems", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--adjoint-problems", type=int, default=16)
@@ -368,6 +370,45 @@ def fp32_measure(hg, _abi, ic, args):
                                             "E": float(err[3])}}
 
 
+def gravity_measure(hg, _abi, ic, args):
+    """Self-gravity workload: `gravity_size`^2 (ghosts included) EulerRoe FP64 RK4 MinMod,
+    periodic, useGravity with gaussSeidelMaxIter 20 and G = 1 (the reference's defaults,
+    res/config.lua:65-74), three seeded Gaussian over-densities at rest (p = 10).  Whole
+    steps (Roe pass + self-gravity pass with 4 x 20 relaxation sweeps) timed with CUDA
+    events over graph replays; the per-kernel breakdown from event pairs; the
+    relaxation sweep's HBM fraction with 32 algorithmic bytes per interior cell and
+    sweep (the potential read once per colour, written once, the density read once)."""
+    n = args.gravity_size
+    cfg = _abi.make_config(solver="EulerRoe", size=(n, n), boundary="PERIODIC", limiter="MinMod",
+                           integrator="RungeKutta4", use_gravity=True, gauss_seidel_max_iter=20,
+                           gravitational_constant=1.)
+    s_ = hg.Solver(cfg)
+    t0 = time.perf_counter()
+    s_.resetState(ic.gravity_blobs(size=(n, n), seed=7))
+    reset_s = time.perf_counter() - t0
+    s_.update(args.warmup, want_dt=False)
+    ms = s_.timed_update(args.steps) / args.steps
+    prof = s_.profile(2)
+    kps = s_.kernels_per_step()
+    health = s_.health()
+    s_.close()
+    interior = (n - 4) * (n - 4)
+    total = sum(v[1] for v in prof.values())
+    breakdown = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / total} for k, v in prof.items()}
+    relax = prof.get("poisson_relax")
+    peak_gbs, peak_kind = measured_peaks()
+    sweep_ms = relax[1] / relax[0] if relax else None
+    sweep = None
+    if sweep_ms:
+        gbs = 32. * interior / (sweep_ms * 1e-3) / 1e9
+        sweep = {"ms_per_sweep": sweep_ms, "algorithmic_bytes_per_sweep": 32 * interior, "achieved": gbs,
+                 "peak": peak_gbs, "unit": "GB/s", "frac": gbs / peak_gbs, "peak_source": peak_kind}
+    return {"workload": "self-gravitating blobs %dx%d, EulerRoe FP64 RK4 MinMod periodic, useGravity, "
+                        "gaussSeidelMaxIter 20, G 1" % (n, n),
+            "value": interior / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "kernels_per_step": kps,
+            "reset_s": reset_s, "relax_sweep": sweep, "kernels": breakdown, "health_flags": health}
+
+
 def adjoint_measure(hg, _abi, ic, args):
     """Adjoint workload: Kelvin-Helmholtz 512^2 problems (seeds 100..), EulerRoe FP64
     RK2 MinMod periodic, `adjoint_steps` steps with CFL dt recorded and then frozen,
@@ -551,13 +592,15 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_sample(size)
 
-    batched = adjoint = fp32 = None
+    batched = adjoint = fp32 = gravity = None
     if rank == 0 and world == 1:
         fp32 = fp32_measure(hg, _abi, ic, args)
     if rank == 0 and world == 1 and not args.no_batch:
         batched = batched_sweep(hg, _abi, ic, args)
     if rank == 0 and world == 1 and not args.no_adjoint:
         adjoint = adjoint_measure(hg, _abi, ic, args)
+    if rank == 0 and world == 1 and not args.no_gravity:
+        gravity = gravity_measure(hg, _abi, ic, args)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -576,6 +619,7 @@ def run_gb300(args):
         "fp32": fp32,
         "batched_sweep": batched,
         "adjoint": adjoint,
+        "self_gravity": gravity,
         "gpu_launches": kernels_per_step * args.steps,
         "health_flags": health,
     }

@@ -388,6 +388,7 @@ void Solver<real>::initBuffers() {                           // Solver::initBuff
     healthBuf = DeviceBuffer(sizeof(unsigned), true);
     health = healthBuf.as<unsigned>();
     potential = DeviceBuffer(sizeof(real) * (size_t)rc.grid.V, true);
+    if (rc.cfg.use_gravity) relaxRhs = DeviceBuffer(sizeof(double) * (size_t)rc.grid.V, true);
 }
 
 // Converter::toGPU (Solver.cpp:333-337) then SelfGravitation::resetState
@@ -411,24 +412,33 @@ void Solver<real>::resetState(const void* host, size_t count, const void* pot) {
         cudaCheck(cudaMemsetAsync(potential.get(), 0, sizeof(real) * V, stream), "zero potential");
     launchPotentialInit<real>(rc.grid, rc.cfg.use_gravity ? 1 : 0, state.as<real>(), potential.as<real>(), stream);
     potentialLive_ = rc.cfg.use_gravity || nonzero;
-    if (rc.cfg.use_gravity) {
-        // the relaxation reads the density, which the energy update above does not touch
-        for (int tries = 0; tries < 100; ++tries) relaxPotential(state.as<real>(), rc.cfg.gauss_seidel_max_iter);
-    }
+    // 100 x gaussSeidelMaxIter relaxations; they read the density, which the energy
+    // update above does not touch
+    if (rc.cfg.use_gravity) relaxPotential(state.as<real>(), 100 * rc.cfg.gauss_seidel_max_iter);
     cudaCheck(cudaGetLastError(), "reset kernels");
     cudaCheck(cudaStreamSynchronize(stream), "set_state sync");
 }
 
+// `sweeps` x (potentialBoundary, relax) (SelfGravitation.cpp:81-86, 112-117).  The
+// relaxation reads and writes interior cells only and the ghost fill writes ghosts only,
+// so the ghosts end up as the last fill leaves them and the interior as the sweeps do:
+// sweeps-1 relaxations, one fill, one relaxation give the same bits.
 template <typename real>
 void Solver<real>::relaxPotential(const real* densitySource, int sweeps) {
-    for (int i = 0; i < sweeps; ++i) {
-        launch("potential_boundary", rc.dim, [&] {
-            launchPotentialBoundary<real>(rc.grid, methods, potential.as<real>(), stream);
-        });
+    if (sweeps <= 0) return;
+    launch("poisson_relax_rhs", 1, [&] {
+        launchRelaxRhs<real>(rc.grid, gc, densitySource, relaxRhs.template as<double>(), stream);
+    });
+    auto sweep = [&] {
         launch("poisson_relax", 2, [&] {
-            launchRelaxSweep<real>(rc.grid, gc, densitySource, potential.as<real>(), stream);
+            launchRelaxSweep<real>(rc.grid, gc, relaxRhs.template as<double>(), potential.as<real>(), stream);
         });
-    }
+    };
+    for (int i = 0; i < sweeps - 1; ++i) sweep();
+    launch("potential_boundary", rc.dim, [&] {
+        launchPotentialBoundary<real>(rc.grid, methods, potential.as<real>(), stream);
+    });
+    sweep();
 }
 
 template <typename real>

@@ -221,6 +221,7 @@ public:
     Phys<real> ph;
     DeviceBuffer state, flux, stepConst, dtAcc, healthBuf;
     DeviceBuffer potential;                 // SelfGravitation::potentialBuffer (V values)
+    DeviceBuffer relaxRhs;                  // 4 pi G density of the state being relaxed against (double)
     GravityConst<real> gc;                  // relaxation / gravity-source constants
     // the potential the flux kernels see: null while it is zero (its terms change no bit)
     const real* livePotential() const { return potentialLive_ ? potential.as<real>() : nullptr; }

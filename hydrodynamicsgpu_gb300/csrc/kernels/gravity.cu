@@ -50,41 +50,56 @@ __global__ void __launch_bounds__(kThreads) potentialBoundaryKernel(Grid g, int 
     boundaryLine<real>(g, axis, 1, mMin, mMax, pot, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// one colour of a relaxation sweep: thread t -> the t-th interior cell of that colour
+// rhs = 4. * M_PI * G * density (double) of every cell, from the stage state: fixed
+// while a callback's sweeps run, so it is formed once and the sweeps read 8 bytes a
+// cell instead of the state's record
+template <typename real, int D>
+__global__ void __launch_bounds__(kThreads) relaxRhsKernel(Grid g, GravityConst<real> gc,
+                                                           const real* __restrict__ state, double* __restrict__ rhs) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.V) return;
+    rhs[c] = mulI(gc.fourPiG, (double)state[(long long)(D + 2) * c]);
+}
+
+// x / dx^2 of the relaxation, exact: FP64 by the quotient correction on RN(1 / dx^2)
+// (fp64ops.cuh divByRecip: two FMAs on the FP64 unit) or on the integer pipes (divI);
+// FP32 the float division.  Measured on GB300 (2048^2 sweep): the x neighbours by the
+// correction and the rest on the integer pipes balance the two units best (0.134 ms a
+// sweep; all on the integer pipes 0.168, every neighbour by the correction 0.154).
+template <bool RECIP>
+__device__ __forceinline__ double overDxSq(double x, double d, double rd) {
+    return RECIP ? divByRecip(x, d, rd) : divI(x, d);
+}
+template <bool RECIP>
+__device__ __forceinline__ float overDxSq(float x, float d, double) { return x / d; }
+
+// one colour of a relaxation sweep: blockIdx.y (+ gridDim.y * blockIdx.z) = the interior
+// row (y, z), thread x = the k-th cell of that colour along the row
 template <typename real, int D>
 __global__ void __launch_bounds__(kThreads) relaxKernel(Grid g, GravityConst<real> gc, int colour,
-                                                        const real* __restrict__ state, real* __restrict__ pot) {
-    // interior extents and the colour's cells per x-row (x from 2 to S0-3)
-    const int nx = g.S[0] - 4, ny = D > 1 ? g.S[1] - 4 : 1, nz = D > 2 ? g.S[2] - 4 : 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int halfRow = (nx + 1) / 2;                        // cells of one colour per row (upper bound)
-    const long long rows = (long long)ny * nz;
-    if (t >= rows * halfRow) return;
-    const int r = (int)(t / halfRow), k = (int)(t % halfRow);
-    const int iy = r % ny, iz = r / ny;
-    const int y = D > 1 ? iy + 2 : 0, z = D > 2 ? iz + 2 : 0;
+                                                        const double* __restrict__ rhs, real* __restrict__ pot) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = D > 1 ? (int)blockIdx.y + 2 : 0, z = D > 2 ? (int)blockIdx.z + 2 : 0;
     // x = 2 + 2k + shift, with shift chosen so that x + y + z has the colour's parity
-    const int shift = ((2 + y + z) & 1) ^ colour;
-    const int x = 2 + 2 * k + shift;
+    const int x = 2 + 2 * k + (((y + z) & 1) ^ colour);
     if (x >= g.S[0] - 2) return;
     const long long c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
     // skewSum: +x, -x, +y, -y, +z, -z neighbours inside [2, S-3] (SelfGravitation.cl:39-51)
     real skewSum = (real)0;
-    if (x < g.S[0] - 3) skewSum = skewSum + divI(pot[c + 1], gc.dxSq[0]);
-    if (x > 2) skewSum = skewSum + divI(pot[c - 1], gc.dxSq[0]);
+    if (x < g.S[0] - 3) skewSum = skewSum + overDxSq<true>(pot[c + 1], gc.dxSq[0], gc.rdxSq[0]);
+    if (x > 2) skewSum = skewSum + overDxSq<true>(pot[c - 1], gc.dxSq[0], gc.rdxSq[0]);
     if (D > 1) {
         const long long sy = g.step[1];
-        if (y < g.S[1] - 3) skewSum = skewSum + divI(pot[c + sy], gc.dxSq[1]);
-        if (y > 2) skewSum = skewSum + divI(pot[c - sy], gc.dxSq[1]);
+        if (y < g.S[1] - 3) skewSum = skewSum + overDxSq<false>(pot[c + sy], gc.dxSq[1], gc.rdxSq[1]);
+        if (y > 2) skewSum = skewSum + overDxSq<false>(pot[c - sy], gc.dxSq[1], gc.rdxSq[1]);
     }
     if (D > 2) {
         const long long sz = g.step[2];
-        if (z < g.S[2] - 3) skewSum = skewSum + divI(pot[c + sz], gc.dxSq[2]);
-        if (z > 2) skewSum = skewSum + divI(pot[c - sz], gc.dxSq[2]);
+        if (z < g.S[2] - 3) skewSum = skewSum + overDxSq<false>(pot[c + sz], gc.dxSq[2], gc.rdxSq[2]);
+        if (z > 2) skewSum = skewSum + overDxSq<false>(pot[c - sz], gc.dxSq[2], gc.rdxSq[2]);
     }
-    const real density = state[(long long)(D + 2) * c];
     // (4. * M_PI * G * density - skewSum) / diag, in double for both precisions
-    pot[c] = (real)divI(mulI(gc.fourPiG, (double)density) - (double)skewSum, gc.diag);
+    pot[c] = (real)divI(rhs[c] - (double)skewSum, gc.diag);
 }
 
 // calcGravityDeriv of one cell into d (zero outside the interior), then the combine
@@ -134,10 +149,11 @@ GravityConst<real> gravityConst(const double dx[3], double G, int dim) {
         const real dxr = (real)dx[i];
         const real sq = dxr * dxr;                                  // DX * DX in the program's type
         gc.dxSq[i] = sq;
+        gc.rdxSq[i] = 1. / (double)sq;                                // RN(1 / dx^2) for the exact quotient
         invSum = i == 0 ? 1. / (double)sq : invSum + 1. / (double)sq;
         gc.twoDx[i] = 2. * (double)dxr;
     }
-    for (int i = dim; i < 3; ++i) { gc.dxSq[i] = (real)1; gc.twoDx[i] = 2.; }
+    for (int i = dim; i < 3; ++i) { gc.dxSq[i] = (real)1; gc.rdxSq[i] = 1.; gc.twoDx[i] = 2.; }
     gc.diag = (double)(real)(-2. * invSum);                          // `const real diag`
     return gc;
 }
@@ -161,14 +177,21 @@ void launchPotentialBoundary(const Grid& g, const int methods[3][2], real* pot, 
 }
 
 template <typename real>
-void launchRelaxSweep(const Grid& g, const GravityConst<real>& gc, const real* state, real* pot, cudaStream_t st) {
-    const long long nx = g.S[0] - 4, ny = g.dim > 1 ? g.S[1] - 4 : 1, nz = g.dim > 2 ? g.S[2] - 4 : 1;
+void launchRelaxRhs(const Grid& g, const GravityConst<real>& gc, const real* state, double* rhs, cudaStream_t st) {
+    if (g.dim == 1) relaxRhsKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, gc, state, rhs);
+    else if (g.dim == 2) relaxRhsKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, gc, state, rhs);
+    else relaxRhsKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, gc, state, rhs);
+}
+
+template <typename real>
+void launchRelaxSweep(const Grid& g, const GravityConst<real>& gc, const double* rhs, real* pot, cudaStream_t st) {
+    const int nx = g.S[0] - 4, ny = g.dim > 1 ? g.S[1] - 4 : 1, nz = g.dim > 2 ? g.S[2] - 4 : 1;
     if (nx <= 0 || ny <= 0 || nz <= 0) return;
-    const long long n = ny * nz * ((nx + 1) / 2);
+    const dim3 grid((unsigned)((nx + 1) / 2 + kThreads - 1) / kThreads, (unsigned)ny, (unsigned)nz);
     for (int colour = 0; colour < 2; ++colour) {
-        if (g.dim == 1) relaxKernel<real, 1><<<blocksFor(n), kThreads, 0, st>>>(g, gc, colour, state, pot);
-        else if (g.dim == 2) relaxKernel<real, 2><<<blocksFor(n), kThreads, 0, st>>>(g, gc, colour, state, pot);
-        else relaxKernel<real, 3><<<blocksFor(n), kThreads, 0, st>>>(g, gc, colour, state, pot);
+        if (g.dim == 1) relaxKernel<real, 1><<<grid, kThreads, 0, st>>>(g, gc, colour, rhs, pot);
+        else if (g.dim == 2) relaxKernel<real, 2><<<grid, kThreads, 0, st>>>(g, gc, colour, rhs, pot);
+        else relaxKernel<real, 3><<<grid, kThreads, 0, st>>>(g, gc, colour, rhs, pot);
     }
 }
 
@@ -184,7 +207,8 @@ void launchGravityCombine(const Grid& g, const GravityConst<real>& gc, const rea
     template GravityConst<real> gravityConst<real>(const double[3], double, int);                              \
     template void launchPotentialInit<real>(const Grid&, int, real*, real*, cudaStream_t);                      \
     template void launchPotentialBoundary<real>(const Grid&, const int[3][2], real*, cudaStream_t);            \
-    template void launchRelaxSweep<real>(const Grid&, const GravityConst<real>&, const real*, real*, cudaStream_t); \
+    template void launchRelaxRhs<real>(const Grid&, const GravityConst<real>&, const real*, double*, cudaStream_t); \
+    template void launchRelaxSweep<real>(const Grid&, const GravityConst<real>&, const double*, real*, cudaStream_t); \
     template void launchGravityCombine<real>(const Grid&, const GravityConst<real>&, const real*, const real*,    \
                                              const CombinePlan<real>&, const StepConst<real>*, cudaStream_t);
 INST(double)
