@@ -149,8 +149,14 @@ __device__ __forceinline__ double divI(double x, double y) {
     const unsigned s = mx < d;
     e -= (int)s;
     const unsigned long long dn = d << 11;                                   // [2^63, 2^64)
-    const float rf = __frcp_rn((float)(unsigned)(dn >> 40));                // exact operand in [2^23, 2^24)
-    unsigned long long v = __float2ull_rz(rf * 7.737125245533627e25f);       // rf * 2^86, in (2^62, 2^63]
+    // The seed's two conversions are exact and done on the bits (the conversion
+    // instructions would issue to the FP64 unit): the top 24 bits t in [2^23, 2^24)
+    // are the float with exponent field 150 and fraction t - 2^23; rf = RN(1/t) lies
+    // in (2^-24, 2^-23], so rf * 2^86 = (its 24-bit significand) << (exponent field - 64).
+    const unsigned top = (unsigned)(dn >> 40);
+    const float rf = __frcp_rn(__uint_as_float((150u << 23) | (top & 0x7FFFFFu)));
+    const unsigned rb = __float_as_uint(rf);
+    unsigned long long v = (unsigned long long)((rb & 0x7FFFFFu) | 0x800000u) << (((rb >> 23) & 0xFFu) - 64u);
 #pragma unroll
     for (int it = 0; it < 2; ++it) {
         const unsigned long long plo = dn * v, phi = __umul64hi(dn, v);
