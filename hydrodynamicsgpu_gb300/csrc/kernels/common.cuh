@@ -91,9 +91,21 @@ enum : unsigned int { HEALTH_NONFINITE_DT = 1u, HEALTH_HLLC_NOBRANCH = 2u };
 // Literal types follow the reference source: `2.` is a double literal, so in the FP32
 // program those sub-expressions are evaluated in double and converted back, exactly
 // as C/OpenCL promote them; the FP64 program is unaffected.
+// MinMod, max(0, min(r, 1)) with those semantics, decided on the bit pattern: NaN and
+// r >= 1 give 1, [+0, 1) gives r, -0 gives -0 (fmax(0, -0) is its second operand), any
+// other negative gives +0.  (Through fminLibm/fmaxLibm the compiler issues FP64
+// instructions for it; this form stays on the integer pipes.)
+__device__ __forceinline__ double minmodBits(double r) {
+    const long long b = bitsOf(r), one = 0x3FF0000000000000LL;   // the bits of 1.
+    const long long out = (isNaNBits(r) || b >= one) ? one : ((b >= 0 || b == (long long)0x8000000000000000ULL) ? b : 0LL);
+    return fromBits(out);
+}
+__device__ __forceinline__ float minmodBits(float r) { return fmaxLibm(0.f, fminLibm(r, 1.f)); }
+
 template <typename real>
 __device__ __forceinline__ real slopeLimiter(int lim, real r) {
     typedef double W;
+    if (lim == 8) return minmodBits(r);                                                         // MinMod
 #define MN fminLibm
 #define MX fmaxLibm
     switch (lim) {

@@ -25,12 +25,15 @@ __device__ __forceinline__ bool geZero(double x) {
 }
 __device__ __forceinline__ bool geZero(float x) { return x >= 0.f; }
 
-// .5 * x exactly: decrement the exponent of a normal x whose half is normal.
+// .5 * x exactly: decrement the exponent of a normal x whose half is normal.  The
+// rare other operands (zero, subnormal, Inf, NaN) take the FP64 unit out of line, so
+// the compiler cannot issue that product for every operand and select.
+static __device__ __noinline__ double halfNative(double x) { return x * .5; }
 __device__ __forceinline__ double halfOf(double x) {
     long long b = bitsOf(x);
     int e = (int)((b >> 52) & 0x7FF);
     if (e >= 2 && e <= 0x7FE) return fromBits(b - (1LL << 52));
-    return x * .5;
+    return halfNative(x);
 }
 __device__ __forceinline__ float halfOf(float x) { return x * .5f; }
 
@@ -38,20 +41,24 @@ __device__ __forceinline__ float halfOf(float x) { return x * .5f; }
 __device__ __forceinline__ long long orderKey(long long b) { return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL); }
 
 // C library fmin/fmax semantics (the oracle's): a NaN operand yields the other
-// operand; equal operands (including -0 and +0) yield the second one.
+// operand; equal operands (including -0 and +0) yield the second one.  The choice is
+// made on the bit patterns and the result selected as an integer: a select between
+// two doubles issues FP64-unit instructions on this part.
 __device__ __forceinline__ double fminLibm(double x, double y) {
-    long long bx = bitsOf(x), by = bitsOf(y);
-    if (isNaNBits(y)) return x;
-    if (isNaNBits(x)) return y;
-    bool bothZero = ((bx | by) & 0x7FFFFFFFFFFFFFFFLL) == 0;
-    return (!bothZero && orderKey(bx) < orderKey(by)) ? x : y;
+    const long long bx = bitsOf(x), by = bitsOf(y);
+    const bool bothZero = ((bx | by) & 0x7FFFFFFFFFFFFFFFLL) == 0;
+    const bool takeX = isNaNBits(y) || (!isNaNBits(x) && !bothZero && orderKey(bx) < orderKey(by));
+    return fromBits(takeX ? bx : by);
 }
 __device__ __forceinline__ double fmaxLibm(double x, double y) {
-    long long bx = bitsOf(x), by = bitsOf(y);
-    if (isNaNBits(y)) return x;
-    if (isNaNBits(x)) return y;
-    bool bothZero = ((bx | by) & 0x7FFFFFFFFFFFFFFFLL) == 0;
-    return (!bothZero && orderKey(bx) > orderKey(by)) ? x : y;
+    const long long bx = bitsOf(x), by = bitsOf(y);
+    const bool bothZero = ((bx | by) & 0x7FFFFFFFFFFFFFFFLL) == 0;
+    const bool takeX = isNaNBits(y) || (!isNaNBits(x) && !bothZero && orderKey(bx) > orderKey(by));
+    return fromBits(takeX ? bx : by);
+}
+// c ? 1. : -1., selected as an integer
+__device__ __forceinline__ double plusMinusOne(bool c) {
+    return fromBits(c ? 0x3FF0000000000000LL : (long long)0xBFF0000000000000ULL);
 }
 __device__ __forceinline__ float fminLibm(float x, float y) { return (x < y || y != y) ? x : y; }
 __device__ __forceinline__ float fmaxLibm(float x, float y) { return (x > y || y != y) ? x : y; }

@@ -329,7 +329,7 @@ __device__ __forceinline__ void roeFluxCorrections(const double* rec, const doub
     const int N = D + 2;
     const double vx = rec[R_::VX];
     const bool midUp = geZero(vx);
-    const double midTheta = midUp ? 1. : -1.;
+    const double midTheta = plusMinusOne(midUp);
     const double midEpsTheta = mulI(vx, dt_dx) - midTheta;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -337,7 +337,7 @@ __device__ __forceinline__ void roeFluxCorrections(const double* rec, const doub
         const double eigenvalue = roeEigenvalue<double, D>(rec, i);
         const bool up = mid ? midUp : geZero(eigenvalue);
         const double rTilde = divI(up ? dqL[i] : dqR[i], dq[i]);
-        const double theta = mid ? midTheta : (up ? 1. : -1.);
+        const double theta = plusMinusOne(up);
         const double phi = slopeLimiter<double>(LIM >= 0 ? LIM : lim, rTilde);
         const double epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
         const double A = theta + phi * epsMinusTheta;
