@@ -45,9 +45,10 @@ __device__ __forceinline__ void loadParams(const double* __restrict__ B, long lo
     p.hm = b[R_::HM * V];
     p.hp = b[R_::HP * V];
     p.hv2 = b[R_::HV2 * V];
-    p.vv = 2. * p.hv2;
-    p.c = .5 * (p.lamE - p.lam0);
-    p.H = .5 * (p.hm + p.hp);
+    // (scalings by 1/2 and 2 by the exponent, exact, on the integer pipes)
+    p.vv = p.hv2 + p.hv2;
+    p.c = halfOf(p.lamE - p.lam0);
+    p.H = halfOf(p.hm + p.hp);
     p.id = divI(.5, p.c * p.c);
 }
 
@@ -62,12 +63,12 @@ __device__ __forceinline__ void leftVJP(const FaceParams<D>& p, double gm1, cons
         vtx += p.vt[t] * x[2 + t];
         gvt += g[2 + t] * p.vt[t];
     }
-    const double Q = gm1 * (.5 * p.vv * x[0] - p.vx * x[1] - vtx + x[E]);
+    const double Q = gm1 * (p.hv2 * x[0] - p.vx * x[1] - vtx + x[E]);        // .5 vv = hv2
     const double W = p.vx * x[0] - x[1];
     const double a = (g[0] + g[E] - 2. * g[1]) * p.id;
     const double b = (g[0] - g[E]) * p.id * p.c;
     const double ag = a * gm1;
-    gx[0] = ag * .5 * p.vv + b * p.vx + g[1] - gvt;
+    gx[0] = ag * p.hv2 + b * p.vx + g[1] - gvt;
     gx[1] = -ag * p.vx - b;
 #pragma unroll
     for (int t = 0; t < D - 1; ++t) gx[2 + t] = -ag * p.vt[t] + g[2 + t];
@@ -97,7 +98,7 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
     for (int j = 0; j < N; ++j) {
         const int pj = perm<SIDE>(j);
         gn[j] = (gFc[pj] - gFl[pj]) * rdx;
-        avg[j] = .5 * (U[N * (c - st) + pj] + U[N * c + pj]);
+        avg[j] = halfOf(U[N * (c - st) + pj] + U[N * c + pj]);
     }
     const double* T = FT + (long long)SIDE * FT_PLANES * N * V + c;
     double ft[N];
@@ -131,24 +132,25 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
         // d/dlam = y - h A - h lam phi k,  d/ddq0 = -lam A / 2,  d/dphi = -h lam (lam k - theta)
         const double lam = i == 0 ? p.lam0 : (i == E ? p.lamE : p.vx);
         const bool up = geZero(lam);
-        const double em = lam * k - (up ? 1. : -1.);
+        const double em = lam * k - plusMinusOne(up);
         const double dq0 = DQ[((long long)SIDE * N + i) * V + c];
         const double y = T[((long long)FT_Y * N + i) * V], A = T[((long long)FT_A * N + i) * V];
         const double phi = T[((long long)FT_PHI * N + i) * V], dphi = T[((long long)FT_DPHI * N + i) * V];
-        const double gf = gft[i], t = lam * gf, h = .5 * dq0;
+        const double gf = gft[i], t = lam * gf, h = halfOf(dq0);
         gy[i] = t;
         const double gLam = gf * y - h * (A * gf + phi * k * t);
-        gq0[i] = -.5 * A * t;
+        gq0[i] = -halfOf(A * t);
         gqM[i] = 0.;
         gqP[i] = 0.;
         const double gphi = -h * em * t;
-        if (dphi != 0. && isfinite(dphi)) {
+        // (tests and selects on the bits: double compares and selects issue to the FP64 unit)
+        if (finiteNonzeroD(dphi)) {
             const double r = T[((long long)FT_R * N + i) * V];
-            if (isfinite(r)) {
+            if (finiteD(r)) {
                 const double gUp = gphi * dphi * divI(1., dq0);
                 gq0[i] -= gUp * r;
-                if (up) gqM[i] = gUp;
-                else gqP[i] = gUp;
+                gqM[i] = selectD(up, gUp, 0.);
+                gqP[i] = selectD(up, 0., gUp);
             }
         }
         gp[0] += gLam;
@@ -161,7 +163,7 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
     const long long o = (long long)SIDE * N * V + c;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        S.gAvg[o + (long long)perm<SIDE>(j) * V] = .5 * gavg[j];
+        S.gAvg[o + (long long)perm<SIDE>(j) * V] = halfOf(gavg[j]);
         S.gdqSelf[o + (long long)j * V] = gq0[j];
         S.gdqToM[o + (long long)j * V] = gqM[j];
         S.gdqToP[o + (long long)j * V] = gqP[j];

@@ -44,21 +44,30 @@ __device__ __forceinline__ long long orderKey(long long b) { return b ^ ((b >> 6
 // operand; equal operands (including -0 and +0) yield the second one.  The choice is
 // made on the bit patterns and the result selected as an integer: a select between
 // two doubles issues FP64-unit instructions on this part.
-__device__ __forceinline__ double fminLibm(double x, double y) {
+__device__ __forceinline__ bool fminTakesFirst(double x, double y) {
     const long long bx = bitsOf(x), by = bitsOf(y);
     const bool bothZero = ((bx | by) & 0x7FFFFFFFFFFFFFFFLL) == 0;
-    const bool takeX = isNaNBits(y) || (!isNaNBits(x) && !bothZero && orderKey(bx) < orderKey(by));
-    return fromBits(takeX ? bx : by);
+    return isNaNBits(y) || (!isNaNBits(x) && !bothZero && orderKey(bx) < orderKey(by));
 }
-__device__ __forceinline__ double fmaxLibm(double x, double y) {
+__device__ __forceinline__ bool fmaxTakesFirst(double x, double y) {
     const long long bx = bitsOf(x), by = bitsOf(y);
     const bool bothZero = ((bx | by) & 0x7FFFFFFFFFFFFFFFLL) == 0;
-    const bool takeX = isNaNBits(y) || (!isNaNBits(x) && !bothZero && orderKey(bx) > orderKey(by));
-    return fromBits(takeX ? bx : by);
+    return isNaNBits(y) || (!isNaNBits(x) && !bothZero && orderKey(bx) > orderKey(by));
 }
+// c ? a : b, selected as an integer
+__device__ __forceinline__ double selectD(bool c, double a, double b) {
+    return fromBits(c ? bitsOf(a) : bitsOf(b));
+}
+__device__ __forceinline__ double fminLibm(double x, double y) { return selectD(fminTakesFirst(x, y), x, y); }
+__device__ __forceinline__ double fmaxLibm(double x, double y) { return selectD(fmaxTakesFirst(x, y), x, y); }
 // c ? 1. : -1., selected as an integer
 __device__ __forceinline__ double plusMinusOne(bool c) {
     return fromBits(c ? 0x3FF0000000000000LL : (long long)0xBFF0000000000000ULL);
+}
+// x is finite / x is finite and nonzero, on the bits
+__device__ __forceinline__ bool finiteD(double x) { return (bitsOf(x) & 0x7FF0000000000000LL) != 0x7FF0000000000000LL; }
+__device__ __forceinline__ bool finiteNonzeroD(double x) {
+    return finiteD(x) && (bitsOf(x) & 0x7FFFFFFFFFFFFFFFLL) != 0;
 }
 __device__ __forceinline__ float fminLibm(float x, float y) { return (x < y || y != y) ? x : y; }
 __device__ __forceinline__ float fmaxLibm(float x, float y) { return (x > y || y != y) ? x : y; }

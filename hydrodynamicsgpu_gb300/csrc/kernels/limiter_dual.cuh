@@ -23,20 +23,21 @@ __device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a
 __device__ __forceinline__ Dual operator/(double a, Dual b) { return cst(a) / b; }
 __device__ __forceinline__ Dual dabs(Dual a) { return signbit(a.v) ? Dual{-a.v, -a.d} : a; }
 // the operand fminLibm / fmaxLibm return: NaN yields the other, ties the second
-__device__ __forceinline__ Dual dmin(Dual a, Dual b) {
-    if (b.v != b.v) return a;
-    if (a.v != a.v) return b;
-    return a.v < b.v ? a : b;
-}
-__device__ __forceinline__ Dual dmax(Dual a, Dual b) {
-    if (b.v != b.v) return a;
-    if (a.v != a.v) return b;
-    return a.v > b.v ? a : b;
-}
+// (chosen on the bits and selected as integers, like fminLibm / fmaxLibm)
+__device__ __forceinline__ Dual dsel(bool c, Dual a, Dual b) { return {selectD(c, a.v, b.v), selectD(c, a.d, b.d)}; }
+__device__ __forceinline__ Dual dmin(Dual a, Dual b) { return dsel(fminTakesFirst(a.v, b.v), a, b); }
+__device__ __forceinline__ Dual dmax(Dual a, Dual b) { return dsel(fmaxTakesFirst(a.v, b.v), a, b); }
 
 // res/SlopeLimiter.cl, same expressions and min/max operand order as slopeLimiter()
 __device__ __forceinline__ Dual limiterDual(int lim, Dual r) {
     const Dual z = cst(0.), one = cst(1.);
+    if (lim == 8) {
+        // MinMod, max(0, min(r, 1)): the derivative is r's where min takes r and max
+        // takes that, i.e. r in [-0, 1) on the bit pattern (minmodBits for the value)
+        const long long b = bitsOf(r.v);
+        const bool takesR = (b >= 0 && b < 0x3FF0000000000000LL) || b == (long long)0x8000000000000000ULL;
+        return {minmodBits(r.v), selectD(takesR, r.d, 0.)};
+    }
     switch (lim) {
     case 0: return z;
     case 1: return one;
