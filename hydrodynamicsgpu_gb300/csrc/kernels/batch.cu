@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) batchCombineKernel(const BatchProblem<rea
         int x, y, z;
         long long c;
         if (tileCell(pr.g, tl, tu, x, y, z, c))
-            derivCombineCell<real, D>(pr.g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
+            derivCombineCell<real, D, D>(pr.g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
     }
 }
 

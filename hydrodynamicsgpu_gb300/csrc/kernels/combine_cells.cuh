@@ -96,7 +96,11 @@ __device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan
 // Flux divergence and Runge-Kutta combine of one cell (res/CalcFluxDeriv.cl:7-44 and
 // the multAdd chain).  `off` is the cell offset of this grid inside the slot arrays
 // (0 for a single problem; the problem's first cell in a batch).
-template <typename real, int D>
+// RECIP_SIDES: deltaFlux / dx by the exact quotient correction on RN(1/dx) (divByRecip,
+// two FMAs) for the first RECIP_SIDES axes, on the integer pipes (divI) for the rest.
+// Measured: the single-problem kernel is fastest with 1 (0.357 ms a launch at 2048^2,
+// 0.390 with 0, 0.408 with every axis), the batched persistent one with every axis.
+template <typename real, int D, int RECIP_SIDES = 1>
 __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>& ph, const real* __restrict__ flux,
                                                  const CombinePlan<real>& plan, const StepConst<real>& sc,
                                                  long long c, int x, int y, int z, long long off) {
@@ -109,7 +113,8 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
 #pragma unroll
             for (int j = 0; j < N; ++j) {
                 const real* f = flux + ((long long)side * N + j) * g.V + c;
-                real t = divI(f[g.step[side]] - f[0], ph.dx[side]);   // deltaFlux / dx[side]
+                const real df = f[g.step[side]] - f[0];                 // deltaFlux / dx[side]
+                real t = side < RECIP_SIDES ? divByRecip(df, ph.dx[side], ph.rdx[side]) : divI(df, ph.dx[side]);
                 d[j] = side == 0 ? zfix(-t) : d[j] - t;
             }
         }
