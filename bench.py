@@ -494,9 +494,9 @@ def adjoint_measure(hg, _abi, ic, args):
 # DRAM bytes (read + write) per interior cell of one launch, from the ncu captures in
 # profiles/kernels_kh1024.md (KH 1024x1024, same kernels); traffic grows with the cells
 # processed, so the bench workload's per-launch traffic is this times its interior cells.
-# roe_flux is its two passes together (corrections 147 B + transforms 420 B).
-MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 567.0, "roe_delta_q_tilde": 253.0, "roe_eigenbasis": 245.0,
-                             "flux_divergence_combine": 126.0}
+# roe_flux is its two passes together (corrections 148 B + transforms 420 B).
+MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 568.0, "roe_delta_q_tilde": 252.0, "roe_eigenbasis": 245.0,
+                             "flux_divergence_combine": 123.0}
 
 
 def run_gb300(args):
