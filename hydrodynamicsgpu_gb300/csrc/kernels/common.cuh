@@ -60,8 +60,10 @@ __device__ __forceinline__ float zfix(float x) {
 }
 
 // ---- finiteness by exponent bits (integer pipe) ----
+// Tested on the high 32-bit word: a test of the whole 64-bit pattern is recognised by
+// the compiler as a floating-point class test and issued to the FP64 unit.
 __device__ __forceinline__ bool finiteBits(double x) {
-    return (__double_as_longlong(x) & 0x7FF0000000000000LL) != 0x7FF0000000000000LL;
+    return (__double2hiint(x) & 0x7FF00000) != 0x7FF00000;
 }
 __device__ __forceinline__ bool finiteBits(float x) { return (__float_as_int(x) & 0x7F800000) != 0x7F800000; }
 template <typename real, int N>

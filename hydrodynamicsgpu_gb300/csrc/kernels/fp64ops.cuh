@@ -14,14 +14,22 @@ namespace hgpu {
 __device__ __forceinline__ long long bitsOf(double x) { return __double_as_longlong(x); }
 __device__ __forceinline__ double fromBits(long long b) { return __longlong_as_double(b); }
 
+// Class tests on the two 32-bit words: a test of the whole 64-bit pattern is
+// recognised by the compiler as a floating-point class test or compare and issued to
+// the FP64 unit; on the words it stays on the integer pipes.
 __device__ __forceinline__ bool isNaNBits(double x) {
-    return (bitsOf(x) & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+    const int hi = __double2hiint(x) & 0x7FFFFFFF, lo = __double2loint(x);
+    return hi > 0x7FF00000 || (hi == 0x7FF00000 && lo != 0);
 }
 
 // x >= 0.  (-0 >= 0 is true, NaN >= 0 is false)
 __device__ __forceinline__ bool geZero(double x) {
-    long long b = bitsOf(x);
-    return (b >= 0 && b <= 0x7FF0000000000000LL) || b == (long long)0x8000000000000000ULL;
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    return hi >= 0 ? (hi < 0x7FF00000 || (hi == 0x7FF00000 && lo == 0)) : (hi == (int)0x80000000 && lo == 0);
+}
+// x is +0 or -0
+__device__ __forceinline__ bool isZeroBits(double x) {
+    return ((__double2hiint(x) & 0x7FFFFFFF) | __double2loint(x)) == 0;
 }
 __device__ __forceinline__ bool geZero(float x) { return x >= 0.f; }
 
@@ -64,11 +72,9 @@ __device__ __forceinline__ double fmaxLibm(double x, double y) { return selectD(
 __device__ __forceinline__ double plusMinusOne(bool c) {
     return fromBits(c ? 0x3FF0000000000000LL : (long long)0xBFF0000000000000ULL);
 }
-// x is finite / x is finite and nonzero, on the bits
-__device__ __forceinline__ bool finiteD(double x) { return (bitsOf(x) & 0x7FF0000000000000LL) != 0x7FF0000000000000LL; }
-__device__ __forceinline__ bool finiteNonzeroD(double x) {
-    return finiteD(x) && (bitsOf(x) & 0x7FFFFFFFFFFFFFFFLL) != 0;
-}
+// x is finite / x is finite and nonzero, on the words
+__device__ __forceinline__ bool finiteD(double x) { return (__double2hiint(x) & 0x7FF00000) != 0x7FF00000; }
+__device__ __forceinline__ bool finiteNonzeroD(double x) { return finiteD(x) && !isZeroBits(x); }
 __device__ __forceinline__ float fminLibm(float x, float y) { return (x < y || y != y) ? x : y; }
 __device__ __forceinline__ float fmaxLibm(float x, float y) { return (x > y || y != y) ? x : y; }
 
@@ -123,8 +129,7 @@ __device__ __forceinline__ float mulI(float x, float y) { return x * y; }
 __device__ __forceinline__ double divByRecip(double x, double b, double rb) {
     long long bx = bitsOf(x), bb = bitsOf(b);
     int ex = (int)((bx >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
-    if ((bx & 0x7FFFFFFFFFFFFFFFLL) == 0 && eb != 0 && eb != 0x7FF)
-        return fromBits((bx ^ bb) & (long long)0x8000000000000000ULL);
+    if (isZeroBits(x) && eb != 0 && eb != 0x7FF) return fromBits((bx ^ bb) & (long long)0x8000000000000000ULL);
     if (ex < 623 || ex > 1423 || eb < 623 || eb > 1423) return x / b;
     double q = mulI(x, rb);
     double r = fma(-b, q, x);
