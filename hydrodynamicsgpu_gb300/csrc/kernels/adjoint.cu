@@ -142,12 +142,13 @@ __device__ __forceinline__ void adjFluxFace(const Grid& g, double gm1, int lim, 
         gq0[i] = -halfOf(A * t);
         gqM[i] = 0.;
         gqP[i] = 0.;
-        const double gphi = -h * em * t;
         // (tests and selects on the bits: double compares and selects issue to the FP64 unit)
         if (finiteNonzeroD(dphi)) {
             const double r = T[((long long)FT_R * N + i) * V];
             if (finiteD(r)) {
-                const double gUp = gphi * dphi * divI(1., dq0);
+                // d/d(upwind dq) = gphi phi' / dq0 with gphi = -h em t, h = dq0 / 2: the dq0
+                // cancels (r finite, so dq0 != 0)
+                const double gUp = -halfOf(em * t * dphi);
                 gq0[i] -= gUp * r;
                 gqM[i] = selectD(up, gUp, 0.);
                 gqP[i] = selectD(up, 0., gUp);
@@ -183,7 +184,7 @@ __device__ __forceinline__ void stageCotangent(const AdjStage& st, long long c, 
     for (int i = 0; i < 4; ++i) {                 // constant indices keep `st` in registers
         if (i >= st.nlam) break;
         const double w = st.coefF[i];
-        if (w == 0.) continue;
+        if (isZeroBits(w)) continue;
         const double* l = st.lam[i] + (long long)N * c;
 #pragma unroll
         for (int j = 0; j < N; ++j) out[j] += w * l[j];
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(kT) adjCellsKernel(Grid g, AdjStage st, AdjScr
     for (int i = 0; i < 4; ++i) {
         if (i >= st.nlam) break;
         const double a = st.alpha[i];
-        if (a == 0.) continue;
+        if (isZeroBits(a)) continue;
         const double* l = st.lam[i] + (long long)N * c;
 #pragma unroll
         for (int j = 0; j < N; ++j) acc[j] += a * l[j];
@@ -319,17 +320,18 @@ __device__ __forceinline__ void adjBasisFace(const Grid& g, const Phys<double>& 
     roePrim<double, D>(sL, ph.gamma, L);
     roePrim<double, D>(sR, ph.gamma, R);
     const double norm = divI(1., L.w + R.w);
+    const double wL = L.w * norm, wR = R.w * norm;              // d(average) / d(side value)
     double v[3] = {0., 0., 0.}, vv = 0.;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        v[k] = (L.w * L.v[k] + R.w * R.v[k]) * norm;
+        v[k] = wL * L.v[k] + wR * R.v[k];
         vv += v[k] * v[k];
     }
-    const double H = (L.w * L.h + R.w * R.h) * norm;
-    const double c0 = sqrt((H - .5 * vv) * gm1);
+    const double H = wL * L.h + wR * R.h;
+    const double c0 = sqrt((H - halfOf(vv)) * gm1);
     const double* gP = S.gParam + (long long)SIDE * P * V + c;
     const double gc = gP[(D + 1) * V];
-    const double gcs = divI(gc * gm1 * .5, c0);       // dc/dH; dc/dv_k = -gcs v_k
+    const double gcs = divI(halfOf(gc * gm1), c0);     // dc/dH; dc/dv_k = -gcs v_k
     double gv[3] = {0., 0., 0.};
     gv[SIDE] = gP[0];
     if (D > 1) gv[SIDE == 1 ? 0 : 1] = gP[1 * V];
@@ -346,11 +348,11 @@ __device__ __forceinline__ void adjBasisFace(const Grid& g, const Phys<double>& 
     double* oR = S.gPrimR + (long long)SIDE * P * V + c;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        oL[k * V] = gv[k] * L.w * norm;
-        oR[k * V] = gv[k] * R.w * norm;
+        oL[k * V] = gv[k] * wL;
+        oR[k * V] = gv[k] * wR;
     }
-    oL[D * V] = gH * L.w * norm;
-    oR[D * V] = gH * R.w * norm;
+    oL[D * V] = gH * wL;
+    oR[D * V] = gH * wR;
     oL[(D + 1) * V] = gwL * norm;
     oR[(D + 1) * V] = gwR * norm;
 }
@@ -466,9 +468,9 @@ void launchAdjFlux(const Grid& g, const Phys<double>& ph, int limiter, const dou
                    const double* dq, const double* basis, const double* fluxTape, const AdjStage& st,
                    const AdjScratch& s, int first, cudaStream_t stream) {
 #define L(DD) adjFluxKernel<DD><<<blocksFor(g.V), kT, 0, stream>>>(g, ph, limiter, dtdx[0], dtdx[1], dtdx[2], stage, dq, basis, fluxTape, st, s, first)
-    if (g.dim == 1) L(1);
-    else if (g.dim == 2) L(2);
-    else L(3);
+    if (g.dim == 1) { L(1); }
+    else if (g.dim == 2) { L(2); }
+    else { L(3); }
 #undef L
 }
 
