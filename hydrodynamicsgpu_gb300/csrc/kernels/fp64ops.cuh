@@ -22,6 +22,8 @@ __device__ __forceinline__ bool isNaNBits(double x) {
     return hi > 0x7FF00000 || (hi == 0x7FF00000 && lo != 0);
 }
 
+__device__ __forceinline__ bool isNaNBits(float x) { return x != x; }
+
 // x >= 0.  (-0 >= 0 is true, NaN >= 0 is false)
 __device__ __forceinline__ bool geZero(double x) {
     const int hi = __double2hiint(x), lo = __double2loint(x);
@@ -72,6 +74,14 @@ __device__ __forceinline__ double fmaxLibm(double x, double y) { return selectD(
 __device__ __forceinline__ double plusMinusOne(bool c) {
     return fromBits(c ? 0x3FF0000000000000LL : (long long)0xBFF0000000000000ULL);
 }
+// x <= 0 (-0 and +0 included, NaN false) and a <= b, on the words / bit patterns
+__device__ __forceinline__ bool leZero(double x) { return isZeroBits(x) || (__double2hiint(x) < 0 && !isNaNBits(x)); }
+__device__ __forceinline__ bool leZero(float x) { return x <= 0.f; }
+__device__ __forceinline__ bool leD(double a, double b) {
+    if (isNaNBits(a) || isNaNBits(b)) return false;
+    return (isZeroBits(a) && isZeroBits(b)) || orderKey(bitsOf(a)) <= orderKey(bitsOf(b));
+}
+__device__ __forceinline__ bool leD(float a, float b) { return a <= b; }
 // x is finite / x is finite and nonzero, on the words
 __device__ __forceinline__ bool finiteD(double x) { return (__double2hiint(x) & 0x7FF00000) != 0x7FF00000; }
 __device__ __forceinline__ bool finiteNonzeroD(double x) { return finiteD(x) && !isZeroBits(x); }

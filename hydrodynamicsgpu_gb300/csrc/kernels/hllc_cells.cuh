@@ -61,9 +61,9 @@ __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, do
                                                     mulI(halfOf(mulI(halfOf(halfOf(R.v[0] - L.v[0])),
                                                                      L.density + R.density)),
                                                          cL + cR)));
-    real qL = pressureStar <= L.pressure ? (real)1.
+    real qL = leD(pressureStar, L.pressure) ? (real)1.
                                          : (real)sqrt(1. + mulI(gq, (double)divI(pressureStar, L.pressure) - 1.));
-    real qR = pressureStar <= R.pressure ? (real)1.
+    real qR = leD(pressureStar, R.pressure) ? (real)1.
                                          : (real)sqrt(1. + mulI(gq, (double)divI(pressureStar, R.pressure) - 1.));
     waves[((long long)SIDE * 2 + 0) * g.V + c] = L.v[0] - mulI(cL, qL);
     waves[((long long)SIDE * 2 + 1) * g.V + c] = R.v[0] + mulI(cR, qR);
@@ -135,7 +135,7 @@ __device__ __forceinline__ unsigned long long hllcDtCell(const Grid& g, const Ph
             real minLambda = (real)fminLibm(0., (double)slNext);
             real maxLambda = (real)fmaxLibm(0., (double)srHere);
             real dum = divI(ph.dx[side], maxLambda - minLambda);
-            if (dum != dum) nan = true;
+            if (isNaNBits(dum)) nan = true;
             result = fminLibm(result, dum);
         }
     }
@@ -171,10 +171,11 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
                           L.pressure - R.pressure,
                       mulI(R.density, sr - R.v[0]) - mulI(L.density, sl - L.v[0]));
     bool taken = true;
-    if ((real)0. <= sl) {
+    // (the branch tests on the bit patterns: double compares issue to the FP64 unit)
+    if (geZero(sl)) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fL[i];
-    } else if (sl <= (real)0. && (real)0. <= sStar) {
+    } else if (leZero(sl) && geZero(sStar)) {
         real pressureLR = halfOf(L.pressure + R.pressure + mulI(mulI(L.density, sl - L.v[0]), sStar - L.v[0]) +
                                  mulI(mulI(R.density, sr - R.v[0]), sStar - R.v[0]));
         // every component divides by (sl - sStar): one reciprocal, then exact corrected quotients
@@ -184,7 +185,7 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
 #pragma unroll
         for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(mulI(sStar, mulI(sl, stL[1 + k]) - fL[1 + k]), den, rden);
         flux[E] = divByRecip(mulI(sStar, mulI(sl, stL[E]) - fL[E]) + mulI(mulI(sl, pressureLR), sStar), den, rden);
-    } else if (sStar <= (real)0. && (real)0. <= sr) {
+    } else if (leZero(sStar) && geZero(sr)) {
         real pressureLR = halfOf(L.pressure + R.pressure + mulI(mulI(L.density, sl - L.v[0]), sStar - L.v[0]) +
                                  mulI(mulI(R.density, sr - R.v[0]), sStar - R.v[0]));
         real den = sr - sStar, rden = divI((real)1., den);
@@ -193,7 +194,7 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
 #pragma unroll
         for (int k = 1; k < D; ++k) flux[1 + k] = divByRecip(mulI(sStar, mulI(sr, stR[1 + k]) - fR[1 + k]), den, rden);
         flux[E] = divByRecip(mulI(sStar, mulI(sr, stR[E]) - fR[E]) + mulI(mulI(sr, pressureLR), sStar), den, rden);
-    } else if (sr <= (real)0.) {
+    } else if (leZero(sr)) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fR[i];
     } else {
@@ -236,16 +237,16 @@ __device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, con
     for (int k = 1; k < D; ++k) fR[1 + k] = mulI(mulI(R.density, R.v[k]), R.v[0]);
     fR[E] = mulI(mulI(R.density, R.enthalpyTotal), R.v[0]);
     bool taken = true;
-    if ((real)0. <= sl) {
+    if (geZero(sl)) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fL[i];
-    } else if (sl <= (real)0. && (real)0. <= sr) {
+    } else if (leZero(sl) && geZero(sr)) {
         const real invDenom = (real)divI(1., (double)(sr - sl));
         const real slsr = mulI(sl, sr);
 #pragma unroll
         for (int i = 0; i < N; ++i)
             flux[i] = mulI(mulI(sr, fL[i]) - mulI(sl, fR[i]) + mulI(slsr, stR[i] - stL[i]), invDenom);
-    } else if (sr <= (real)0.) {
+    } else if (leZero(sr)) {
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[i] = fR[i];
     } else {
