@@ -154,12 +154,12 @@ def check(status):
 
 
 class Solver:
-    """A GB300 Euler solver (EulerRoe or EulerHLLC) behind the C ABI.
+    """A GB300 Euler solver (EulerRoe, EulerHLLC or EulerHLL) behind the C ABI.
 
     Mirrors the reference's host interface: construct with a config (the
     HydroGPUApp config fields), ``resetState(state)`` uploads an initial state
     (AoS, ghosts included), ``update(n)`` runs Solver::update n times, ``getState()``
-    downloads it and ``save(prefix)`` writes one raw file per state channel."""
+    downloads it and ``save(directory)`` writes one FITS image per state channel."""
 
     def __init__(self, cfg=None, **kw):
         self.cfg = cfg if cfg is not None else make_config(**kw)
