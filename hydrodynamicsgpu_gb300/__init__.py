@@ -35,6 +35,8 @@ SIGNATURES = {
     "hgpu_get_state": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     "hgpu_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_step": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_update_host": (ctypes.c_int, [_P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_last_dt": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_synchronize": (ctypes.c_int, [_P]),
     "hgpu_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
@@ -237,6 +239,25 @@ class Solver:
         check(lib().hgpu_update(self.h, int(nsteps), ctypes.byref(dt) if want_dt else None))
         self.frame += nsteps
         return dt.value if want_dt else None
+
+    def update_host(self, state, nsteps=1, out=None):
+        """hgpu_update_host: upload `state` (resetState), run `nsteps` updates and
+        download the result into `out` (a new array if None; it may be `state`), the
+        copies overlapped with the first and last step.  Returns (out, last dt).  Use
+        PinnedArray buffers for the overlap."""
+        a = state if (isinstance(state, np.ndarray) and state.dtype == self.dtype and state.flags.c_contiguous) \
+            else np.ascontiguousarray(state, dtype=self.dtype)
+        a = a.reshape(-1)
+        o = out if out is not None else np.empty(self.count, dtype=self.dtype)
+        if o.dtype != self.dtype or not o.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous %s array" % np.dtype(self.dtype).name)
+        if a.size != self.count or o.size != self.count:
+            raise ValueError("state has %d / out %d elements, solver needs %d" % (a.size, o.size, self.count))
+        dt = ctypes.c_double()
+        check(lib().hgpu_update_host(self.h, a.ctypes.data, a.size, int(nsteps), o.ctypes.data, o.size,
+                                     ctypes.byref(dt)))
+        self.frame += nsteps
+        return o, dt.value
 
     def last_dt(self):
         dt = ctypes.c_double()

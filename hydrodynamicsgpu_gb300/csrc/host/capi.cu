@@ -211,6 +211,32 @@ int hgpu_update(hgpu_solver* h, int nsteps, double* last_dt) {
 
 int hgpu_step(hgpu_solver* h, int nsteps, double* last_dt) { return hgpu_update(h, nsteps, last_dt); }
 
+int hgpu_update_host(hgpu_solver* h, const void* host_in, size_t in_count, int nsteps, void* host_out,
+                     size_t out_count, double* last_dt) {
+    if (!h || !host_in || !host_out || nsteps < 1) return fail(HGPU_ERR_ARG, "bad argument");
+    const size_t n = h->s->volume() * (size_t)h->s->numStates();
+    if (in_count != n || out_count != n) return fail(HGPU_ERR_ARG, "state element count mismatch");
+    return guarded([&]() {
+        const bool wasLive = h->s->potentialLive();
+        if (!h->s->hostPipelined()) {
+            h->s->resetState(host_in, in_count, nullptr);
+            if (h->s->potentialLive() != wasLive) destroyGraph(h);
+            runSteps(h, nsteps);
+            h->s->readState(host_out, out_count);
+        } else {
+            h->s->hostStep(host_in, host_out, true, nsteps == 1);
+            if (h->s->potentialLive() != wasLive) destroyGraph(h);   // the step's kernels differ
+            if (nsteps > 1) {
+                runSteps(h, nsteps - 2);
+                h->s->hostStep(nullptr, host_out, false, true);
+            }
+        }
+        const double dt = h->s->lastDt();   // waits for the stream, which waited for the copies
+        if (last_dt) *last_dt = dt;
+        return (int)HGPU_OK;
+    });
+}
+
 int hgpu_last_dt(hgpu_solver* h, double* dt) {
     if (!h || !dt) return fail(HGPU_ERR_ARG, "null argument");
     return guarded([&]() { *dt = h->s->lastDt(); return (int)HGPU_OK; });

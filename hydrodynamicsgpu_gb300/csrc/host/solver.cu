@@ -3,6 +3,7 @@
 // so the launchers' CUDA types resolve); the kernels live in ../kernels/.
 #include "solver.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -294,6 +295,10 @@ void RungeKutta<real>::integrate(const std::function<void(real* stage)>& compute
     for (int k = 0; k < order_; ++k) {
         real* in = plans_[k].slot[inputSlot_[k]];
         computeFlux(in);
+        if (k == order_ - 1 && this->lastCombine) {
+            this->lastCombine(plans_[k]);
+            continue;
+        }
         s->launch("flux_divergence_combine", 1, [&] {
             launchDerivCombine<real>(s->rc.grid, s->ph, s->flux.template as<real>(), plans_[k], s->sc(), s->stream);
         });
@@ -344,6 +349,8 @@ Solver<real>::Solver(const ResolvedConfig& rc_) : rc(rc_) {
 template <typename real>
 Solver<real>::~Solver() {
     integrator.reset();
+    for (cudaEvent_t e : pipeEvents_) cudaEventDestroy(e);
+    if (copyStream_) cudaStreamDestroy(copyStream_);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -473,6 +480,144 @@ template <typename real>
 void Solver<real>::boundary() { boundaryOn(state.as<real>()); }
 
 template <typename real>
+cudaEvent_t Solver<real>::pipeEvent(size_t i) {
+    while (pipeEvents_.size() <= i) {
+        cudaEvent_t e;
+        cudaCheck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event create");
+        pipeEvents_.push_back(e);
+    }
+    return pipeEvents_[i];
+}
+
+template <typename real>
+bool Solver<real>::hostPipelined() const {
+    return rc.dim >= 2 && !rc.cfg.use_fixed_dt && !rc.cfg.use_gravity && bandedPrologue();
+}
+
+// One update() whose state comes from host memory `in` (upload) and/or goes back to
+// host memory `out` (download), with the copies overlapped with the step's own work.
+// The slowest axis (y in 2D, z in 3D) is cut into bands of slow-axis tiles.  Upload:
+// band after band goes up on the copy stream, the last band first (it holds the planes
+// the periodic / mirror / free-flow fill of the first ghost planes reads), then band
+// 0, 1, ...; the solver's stream takes each band as it lands: E += 0 (the zero
+// potential's resetState pass), the ghost fill of the other axes on the band's planes,
+// then the band's share of the eigenbasis, which reads the band's planes and the one
+// below.  The slow axis's own ghost fill runs once the first and last bands are in,
+// before the first band's eigenbasis.  Download: the last stage's combine runs band
+// by band and each band goes down as soon as it is written.  Every cell sees the same
+// operations as in set_state + update + get_state, so the results are the same bits.
+template <typename real>
+void Solver<real>::hostStep(const void* in, void* out, bool upload, bool download) {
+    this->launches_ = 0;
+    if (!copyStream_) cudaCheck(cudaStreamCreateWithFlags(&copyStream_, cudaStreamNonBlocking), "copy stream");
+    const Grid& g = rc.grid;
+    const int A = rc.dim - 1;                                       // slowest axis
+    const long long S_A = g.S[A];
+    const long long plane = (long long)g.V / S_A;                   // cells per slow-axis plane
+    const long long N = rc.numStates;
+    const int T_A = slowTile();
+    const long long tilesA = (S_A + T_A - 1) / T_A;
+    // tiles a band: 128 rows in 2D (measured at 2048^2, ms per update_host step: 4 tiles
+    // 9.99, 8 9.15, 16 8.74, 32 8.71, 64 8.78, 128 9.09; smaller bands cost launches
+    // and partial waves), 16 planes in 3D; at least 4 planes in the first and last band
+    const long long per = std::max<long long>(rc.dim == 2 ? 16 : 8, (4 + T_A - 1) / T_A + 1);
+    const int K = (int)std::max<long long>(1, tilesA / per);
+    auto tile0 = [&](int j) { return (long long)j * per; };
+    auto tile1 = [&](int j) { return j == K - 1 ? tilesA : (long long)(j + 1) * per; };
+    auto plane0 = [&](int j) { return tile0(j) * T_A; };
+    auto plane1 = [&](int j) { return std::min<long long>(tile1(j) * T_A, S_A); };
+    auto bytesOf = [&](long long planes) { return (size_t)(planes * plane * N) * sizeof(real); };
+    auto offOf = [&](long long p) { return (size_t)(p * plane * N) * sizeof(real); };
+    size_t ev = 0;
+    cudaEvent_t start = pipeEvent(ev++);
+    cudaCheck(cudaEventRecord(start, stream), "event record");
+    cudaCheck(cudaStreamWaitEvent(copyStream_, start, 0), "stream wait");   // the state is free to overwrite
+
+    if (upload) {
+        cudaCheck(cudaMemsetAsync(potential.get(), 0, sizeof(real) * (size_t)g.V, stream), "zero potential");
+        potentialLive_ = false;
+        std::vector<cudaEvent_t> landed(K);
+        std::vector<int> order;
+        order.push_back(K - 1);
+        for (int j = 0; j < K - 1; ++j) order.push_back(j);
+        for (int j : order) {
+            cudaCheck(cudaMemcpyAsync(static_cast<char*>(state.get()) + offOf(plane0(j)),
+                                      static_cast<const char*>(in) + offOf(plane0(j)),
+                                      bytesOf(plane1(j) - plane0(j)), cudaMemcpyHostToDevice, copyStream_),
+                      "update_host upload");
+            landed[j] = pipeEvent(ev++);
+            cudaCheck(cudaEventRecord(landed[j], copyStream_), "event record");
+        }
+        auto prep = [&](int j) {
+            cudaCheck(cudaStreamWaitEvent(stream, landed[j], 0), "stream wait");
+            launch("potential_init", 1, [&] {
+                launchPotentialInit<real>(g, 0, state.as<real>(), potential.as<real>(), stream, plane0(j) * plane,
+                                          plane1(j) * plane);
+            });
+            for (int a = 0; a < A; ++a) {
+                // lines of axis a through the band: t = c[T] + S[T] c[U] with U the slow axis
+                // in 3D (S[T] lines a plane), T the slow axis in 2D (one line a plane)
+                const long long perPlane = rc.dim == 2 ? 1 : g.S[a == 0 ? 1 : 0];
+                launch("boundary", 1, [&] {
+                    launchBoundaryAxis<real>(g, methods, state.as<real>(), stream, a, plane0(j) * perPlane,
+                                             plane1(j) * perPlane);
+                });
+            }
+        };
+        prep(K - 1);
+        if (K > 1) prep(0);
+        launch("boundary", 1, [&] { launchBoundaryAxis<real>(g, methods, state.as<real>(), stream, A); });
+        bandedPrologueWork((int)tile0(0), (int)(tile1(0) - tile0(0)));
+        for (int j = 1; j < K - 1; ++j) {
+            prep(j);
+            bandedPrologueWork((int)tile0(j), (int)(tile1(j) - tile0(j)));
+        }
+        if (K > 1) bandedPrologueWork((int)tile0(K - 1), (int)(tile1(K - 1) - tile0(K - 1)));
+        bandedPrologueEnd();
+    } else {
+        boundary();
+        initStep();
+        calcTimestep();
+    }
+    finalizeDt(false);
+
+    const bool banded = download && integrator->lastCombineWritesState();
+    struct Unhook {
+        Integrator<real>* i;
+        ~Unhook() { i->lastCombine = nullptr; }
+    } unhook{integrator.get()};
+    if (banded) {
+        integrator->lastCombine = [&](const CombinePlan<real>& plan) {
+            for (int j = 0; j < K; ++j) {
+                launch("flux_divergence_combine", 1, [&] {
+                    launchDerivCombine<real>(g, ph, flux.template as<real>(), plan, sc(), stream, plane0(j) * plane,
+                                             plane1(j) * plane);
+                });
+                cudaEvent_t written = pipeEvent(ev++);
+                cudaCheck(cudaEventRecord(written, stream), "event record");
+                cudaCheck(cudaStreamWaitEvent(copyStream_, written, 0), "stream wait");
+                cudaCheck(cudaMemcpyAsync(static_cast<char*>(out) + offOf(plane0(j)),
+                                          static_cast<const char*>(state.get()) + offOf(plane0(j)),
+                                          bytesOf(plane1(j) - plane0(j)), cudaMemcpyDeviceToHost, copyStream_),
+                          "update_host download");
+            }
+        };
+    }
+    step();
+    if (download && !banded) {
+        cudaEvent_t stepped = pipeEvent(ev++);
+        cudaCheck(cudaEventRecord(stepped, stream), "event record");
+        cudaCheck(cudaStreamWaitEvent(copyStream_, stepped, 0), "stream wait");
+        cudaCheck(cudaMemcpyAsync(out, state.get(), bytesOf(S_A), cudaMemcpyDeviceToHost, copyStream_),
+                  "update_host download");
+    }
+    cudaEvent_t copied = pipeEvent(ev++);
+    cudaCheck(cudaEventRecord(copied, copyStream_), "event record");
+    cudaCheck(cudaStreamWaitEvent(stream, copied, 0), "stream wait");   // later work may overwrite the state
+    cudaCheck(cudaGetLastError(), "update_host launches");
+}
+
+template <typename real>
 void Solver<real>::finalizeDt(bool fixed) {
     launch("finalize_dt", 1, [&] {
         launchFinalizeDt<real>(ph, rc.cfg.integrator, fixed ? 1 : 0, rc.cfg.fixed_dt, dtAcc.as<unsigned long long>(),
@@ -522,11 +667,26 @@ void Roe<real>::initFlux() {                                 // Roe::initFlux (R
 }
 
 template <typename real>
-void Roe<real>::calcTimestep() {                             // Roe::calcTimestep (Roe.cpp:88-92)
-    initFlux();
+void Roe<real>::cflReduce() {
     this->launch("cfl_min_reduce", 1, [&] {
         launchRoeDt<real>(this->rc.grid, this->ph, basis.template as<real>(),
                           this->dtAcc.template as<unsigned long long>(), this->health, this->stream);
+    });
+}
+
+template <typename real>
+void Roe<real>::calcTimestep() {                             // Roe::calcTimestep (Roe.cpp:88-92)
+    initFlux();
+    cflReduce();
+}
+
+// the eigenbasis of the faces of the band's cells (it reads the band's planes and the
+// plane below the band)
+template <typename real>
+void Roe<real>::bandedPrologueWork(int tile0, int tiles) {
+    this->launch("roe_eigenbasis", 1, [&] {
+        launchRoeBasis<real>(this->rc.grid, this->ph, this->state.template as<real>(), basis.template as<real>(),
+                             this->rc.cfg.compat == HGPU_COMPAT_SEAM, this->stream, nullptr, tile0, tiles);
     });
 }
 

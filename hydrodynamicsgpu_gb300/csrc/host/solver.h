@@ -111,6 +111,11 @@ public:
     virtual void integrateGravity() = 0;
     virtual int order() const = 0;
     virtual int extraBuffers() const = 0;
+    // true when the last stage's combine writes the new state and nothing after it in
+    // the step (the self-gravity pass with a zero potential) touches the state again
+    virtual bool lastCombineWritesState() const { return false; }
+    // when set, the last stage's combine is handed to this instead of launched whole
+    std::function<void(const CombinePlan<real>&)> lastCombine;
 protected:
     Solver<real>* solver;
 };
@@ -135,6 +140,7 @@ public:
     void integrateGravity() override;
     int order() const override { return order_; }
     int extraBuffers() const override { return nslots_; }
+    bool lastCombineWritesState() const override { return alphaIsBinary_; }
 private:
     int tableau_, order_, nslots_ = 0;
     bool alphaIsBinary_ = true;
@@ -188,6 +194,12 @@ public:
     virtual double lastDt() = 0;
     virtual void* stateDevicePtr() = 0;
     virtual int kernelsPerStep() const = 0;
+    // update_host's overlapped form (see Solver<real>::hostStep): supported for this
+    // configuration?  hostStep(in, out, upload, download) is one update() that first
+    // uploads the state from `in` (upload) and/or ends by downloading it into `out`
+    // (download), the copies in bands on a second stream; nothing is synchronised.
+    virtual bool hostPipelined() const = 0;
+    virtual void hostStep(const void* in, void* out, bool upload, bool download) = 0;
     virtual size_t volume() const = 0;
     virtual int dim() const = 0;
     virtual int numStates() const = 0;
@@ -215,6 +227,8 @@ public:
     int dim() const override { return rc.dim; }
     int numStates() const override { return rc.numStates; }
     int kernelsPerStep() const override { return this->launches_; }
+    bool hostPipelined() const override;
+    void hostStep(const void* in, void* out, bool upload, bool download) override;
 
     // accessors used by integrators
     ResolvedConfig rc;
@@ -240,6 +254,22 @@ protected:
     void finalizeDt(bool fixed);
     void applyPotential();                  // SelfGravitation::applyPotential (SelfGravitation.cpp:100-124)
     bool potentialLive_ = false;            // useGravity, or a nonzero static potential was given
+
+    // The step's work before the stages, split in bands along the slowest axis so that
+    // it can start while later bands are still being uploaded.  A solver that supports
+    // it does, for the band of slow-axis tiles [tile0, tile0 + tiles) of slowTile()
+    // planes each, the part of initStep() + calcTimestep() that reads only the planes
+    // of the band and the one below it (bandedPrologueWork), then the rest once every
+    // band is done (bandedPrologueEnd).
+    virtual bool bandedPrologue() const { return false; }
+    virtual int slowTile() const { return 1; }
+    virtual void bandedPrologueWork(int tile0, int tiles) { (void)tile0; (void)tiles; }
+    virtual void bandedPrologueEnd() {}
+
+private:
+    cudaStream_t copyStream_ = nullptr;     // update_host's uploads and downloads
+    std::vector<cudaEvent_t> pipeEvents_;
+    cudaEvent_t pipeEvent(size_t i);
 };
 
 template <typename real>
@@ -258,9 +288,14 @@ protected:
     DeviceBuffer basis, deltaQTilde;
     void initBuffers() override;
     void initFlux();                              // calcEigenBasis once per step
+    void cflReduce();                             // calcCellTimestep + the min-reduction
     void calcTimestep() override;
     void step() override;
     void calcFlux(real* stage);                   // calcDeltaQTilde + calcFlux
+    bool bandedPrologue() const override { return !this->livePotential(); }
+    int slowTile() const override { return roeBasisSlowTile(this->rc.dim); }
+    void bandedPrologueWork(int tile0, int tiles) override;
+    void bandedPrologueEnd() override { cflReduce(); }
 };
 
 template <typename real>

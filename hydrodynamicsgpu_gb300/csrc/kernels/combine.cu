@@ -34,17 +34,20 @@ inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / 
 // ---------------- ghost fill ----------------
 template <typename real>
 __global__ void __launch_bounds__(kThreads) boundaryKernel(Grid g, int axis, int N, int mMin, int mMax,
-                                                           real* __restrict__ state) {
-    boundaryLine<real>(g, axis, N, mMin, mMax, state, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+                                                           real* __restrict__ state, long long t0, long long t1) {
+    const long long t = t0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= t1) return;
+    boundaryLine<real>(g, axis, N, mMin, mMax, state, t);
 }
 
 // ---------------- flux divergence + stage combine ----------------
 template <typename real, int D>
 __global__ void __launch_bounds__(kThreads) derivCombineKernel(Grid g, Phys<real> ph, const real* __restrict__ flux,
                                                                CombinePlan<real> plan,
-                                                               const StepConst<real>* __restrict__ sc) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                               const StepConst<real>* __restrict__ sc, long long c0,
+                                                               long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     derivCombineCell<real, D>(g, ph, flux, plan, *sc, c, x, y, z, 0);
@@ -79,21 +82,36 @@ __global__ void __launch_bounds__(kThreads) zeroAddKernel(long long n, real* __r
 
 }  // namespace
 
+long long boundaryLines(const Grid& g, int axis) {
+    return g.dim == 1 ? 1 : (long long)g.S[axis == 0 ? 1 : 0] * g.S[axis == 2 ? 1 : 2];
+}
+
+template <typename real>
+void launchBoundaryAxis(const Grid& g, const int methods[3][2], real* state, cudaStream_t st, int axis, long long t0,
+                        long long t1) {
+    const long long n = boundaryLines(g, axis);
+    if (t1 < 0 || t1 > n) t1 = n;
+    if (t0 < 0) t0 = 0;
+    if (t0 >= t1) return;
+    boundaryKernel<real><<<blocksFor(t1 - t0), kThreads, 0, st>>>(g, axis, g.dim + 2, methods[axis][0],
+                                                                   methods[axis][1], state, t0, t1);
+}
+
 template <typename real>
 void launchBoundary(const Grid& g, const int methods[3][2], real* state, cudaStream_t st) {
-    const int N = g.dim + 2;
-    for (int axis = 0; axis < g.dim; ++axis) {
-        long long n = g.dim == 1 ? 1 : (long long)g.S[axis == 0 ? 1 : 0] * g.S[axis == 2 ? 1 : 2];
-        boundaryKernel<real><<<blocksFor(n), kThreads, 0, st>>>(g, axis, N, methods[axis][0], methods[axis][1], state);
-    }
+    for (int axis = 0; axis < g.dim; ++axis) launchBoundaryAxis<real>(g, methods, state, st, axis, 0, -1);
 }
 
 template <typename real>
 void launchDerivCombine(const Grid& g, const Phys<real>& ph, const real* flux, const CombinePlan<real>& plan,
-                        const StepConst<real>* sc, cudaStream_t st) {
-    if (g.dim == 1) derivCombineKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, flux, plan, sc);
-    else if (g.dim == 2) derivCombineKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, flux, plan, sc);
-    else derivCombineKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, flux, plan, sc);
+                        const StepConst<real>* sc, cudaStream_t st, long long c0, long long c1) {
+    if (c1 < 0 || c1 > g.V) c1 = g.V;
+    if (c0 < 0) c0 = 0;
+    if (c0 >= c1) return;
+    const unsigned b = blocksFor(c1 - c0);
+    if (g.dim == 1) derivCombineKernel<real, 1><<<b, kThreads, 0, st>>>(g, ph, flux, plan, sc, c0, c1);
+    else if (g.dim == 2) derivCombineKernel<real, 2><<<b, kThreads, 0, st>>>(g, ph, flux, plan, sc, c0, c1);
+    else derivCombineKernel<real, 3><<<b, kThreads, 0, st>>>(g, ph, flux, plan, sc, c0, c1);
 }
 
 template <typename real>
@@ -122,8 +140,10 @@ void launchResetAcc(unsigned long long* acc, unsigned long long accInit, cudaStr
 
 #define INST(real)                                                                                              \
     template void launchBoundary<real>(const Grid&, const int[3][2], real*, cudaStream_t);                      \
+    template void launchBoundaryAxis<real>(const Grid&, const int[3][2], real*, cudaStream_t, int, long long,   \
+                                           long long);                                                          \
     template void launchDerivCombine<real>(const Grid&, const Phys<real>&, const real*, const CombinePlan<real>&, \
-                                           const StepConst<real>*, cudaStream_t);                               \
+                                           const StepConst<real>*, cudaStream_t, long long, long long);         \
     template void launchAlphaOnly<real>(const Grid&, int, real*, const StepConst<real>*, cudaStream_t);         \
     template void launchZeroAdd<real>(const Grid&, real*, const StepConst<real>*, cudaStream_t);                \
     template void launchFinalizeDt<real>(const Phys<real>&, int, int, double, unsigned long long*,              \

@@ -34,9 +34,9 @@ inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / 
 // potential = -density (useGravity) or the given channel; total energy += that potential
 template <typename real, int D>
 __global__ void __launch_bounds__(kThreads) potentialInitKernel(Grid g, int fromDensity, real* __restrict__ state,
-                                                                real* __restrict__ pot) {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                                real* __restrict__ pot, long long c0, long long c1) {
+    const long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     real* s = state + (long long)(D + 2) * c;
     const real p = fromDensity ? -s[0] : pot[c];
     pot[c] = p;
@@ -159,10 +159,15 @@ GravityConst<real> gravityConst(const double dx[3], double G, int dim) {
 }
 
 template <typename real>
-void launchPotentialInit(const Grid& g, int fromDensity, real* state, real* pot, cudaStream_t st) {
-    if (g.dim == 1) potentialInitKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, fromDensity, state, pot);
-    else if (g.dim == 2) potentialInitKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, fromDensity, state, pot);
-    else potentialInitKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, fromDensity, state, pot);
+void launchPotentialInit(const Grid& g, int fromDensity, real* state, real* pot, cudaStream_t st, long long c0,
+                         long long c1) {
+    if (c1 < 0 || c1 > g.V) c1 = g.V;
+    if (c0 < 0) c0 = 0;
+    if (c0 >= c1) return;
+    const unsigned b = blocksFor(c1 - c0);
+    if (g.dim == 1) potentialInitKernel<real, 1><<<b, kThreads, 0, st>>>(g, fromDensity, state, pot, c0, c1);
+    else if (g.dim == 2) potentialInitKernel<real, 2><<<b, kThreads, 0, st>>>(g, fromDensity, state, pot, c0, c1);
+    else potentialInitKernel<real, 3><<<b, kThreads, 0, st>>>(g, fromDensity, state, pot, c0, c1);
 }
 
 template <typename real>
@@ -205,7 +210,7 @@ void launchGravityCombine(const Grid& g, const GravityConst<real>& gc, const rea
 
 #define INST(real)                                                                                              \
     template GravityConst<real> gravityConst<real>(const double[3], double, int);                              \
-    template void launchPotentialInit<real>(const Grid&, int, real*, real*, cudaStream_t);                      \
+    template void launchPotentialInit<real>(const Grid&, int, real*, real*, cudaStream_t, long long, long long);                      \
     template void launchPotentialBoundary<real>(const Grid&, const int[3][2], real*, cudaStream_t);            \
     template void launchRelaxRhs<real>(const Grid&, const GravityConst<real>&, const real*, double*, cudaStream_t); \
     template void launchRelaxSweep<real>(const Grid&, const GravityConst<real>&, const double*, real*, cudaStream_t); \

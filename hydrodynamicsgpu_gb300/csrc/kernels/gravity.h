@@ -17,9 +17,11 @@ struct GravityConst {
 template <typename real>
 GravityConst<real> gravityConst(const double dx[3], double G, int dim);
 
-// potential = -density (fromDensity) or its current contents; total energy += potential
+// potential = -density (fromDensity) or its current contents; total energy += potential;
+// cells [c0, c1) (default: every cell)
 template <typename real>
-void launchPotentialInit(const Grid& g, int fromDensity, real* state, real* pot, cudaStream_t st);
+void launchPotentialInit(const Grid& g, int fromDensity, real* state, real* pot, cudaStream_t st, long long c0 = 0,
+                         long long c1 = -1);
 // SelfGravitation::potentialBoundary: every axis, min then max side
 template <typename real>
 void launchPotentialBoundary(const Grid& g, const int methods[3][2], real* pot, cudaStream_t st);

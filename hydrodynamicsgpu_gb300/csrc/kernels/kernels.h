@@ -38,9 +38,16 @@ struct CombinePlan {
 // ---- boundary.cu ----
 template <typename real>
 void launchBoundary(const Grid& g, const int methods[3][2], real* state, cudaStream_t st);
+// the ghost fill along one axis over its transverse lines [t0, t1) (line t of axis a
+// addresses the cell with c[A] + S[A] * c[B] = t, A < B the other two axes)
+long long boundaryLines(const Grid& g, int axis);
+template <typename real>
+void launchBoundaryAxis(const Grid& g, const int methods[3][2], real* state, cudaStream_t st, int axis,
+                        long long t0 = 0, long long t1 = -1);
+// cells [c0, c1) (default: every cell)
 template <typename real>
 void launchDerivCombine(const Grid& g, const Phys<real>& ph, const real* flux, const CombinePlan<real>& plan,
-                        const StepConst<real>* sc, cudaStream_t st);
+                        const StepConst<real>* sc, cudaStream_t st, long long c0 = 0, long long c1 = -1);
 template <typename real>
 void launchAlphaOnly(const Grid& g, int integrator, real* state, const StepConst<real>* sc, cudaStream_t st);
 template <typename real>
@@ -52,10 +59,13 @@ template <typename real>
 void launchResetAcc(unsigned long long* acc, unsigned long long accInit, cudaStream_t st);
 
 // ---- roe.cu ----
-// pot: the gravitational potential (V values), or null for a zero potential
+// pot: the gravitational potential (V values), or null for a zero potential.  In 2D
+// and 3D, only the tiles [slow0, slow0 + slowTiles) along the slowest axis (y, z) of
+// roeBasisSlowTile(dim) cells each (default: all of them).
 template <typename real>
 void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st,
-                    const real* pot = nullptr);
+                    const real* pot = nullptr, int slow0 = 0, int slowTiles = -1);
+int roeBasisSlowTile(int dim);
 template <typename real>
 void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigned long long* acc, unsigned* health,
                  cudaStream_t st);

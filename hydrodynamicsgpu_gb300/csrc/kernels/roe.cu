@@ -31,15 +31,17 @@ template <> struct BasisTile<1> { enum { X = 256, Y = 1, Z = 1 }; };
 template <> struct BasisTile<2> { enum { X = 32, Y = 8, Z = 1 }; };
 template <> struct BasisTile<3> { enum { X = 32, Y = 4, Z = 2 }; };
 
+// slowOff: tiles skipped along the slowest axis (y in 2D, z in 3D), for a band of it
 template <typename real, int D, bool GRAV>
 __global__ void __launch_bounds__(256) roeBasisKernel(Grid g, Phys<real> ph, const real* __restrict__ state,
                                                      real* __restrict__ basis, int loA, int hiA,
-                                                     const real* __restrict__ pot) {
+                                                     const real* __restrict__ pot, int slowOff) {
     typedef BasisTile<D> T;
     constexpr int HX = T::X + 1, HY = D > 1 ? T::Y + 1 : 1, HZ = D > 2 ? T::Z + 1 : 1;
     __shared__ RoePrim<real, D> prim[HZ * HY * HX];
-    roeBasisTile<real, D, GRAV>(g, ph, state, basis, loA, hiA, blockIdx.x * T::X, blockIdx.y * T::Y,
-                                blockIdx.z * T::Z, T::X, T::Y, T::Z, prim, pot);
+    const int ty = blockIdx.y + (D == 2 ? slowOff : 0), tz = blockIdx.z + (D == 3 ? slowOff : 0);
+    roeBasisTile<real, D, GRAV>(g, ph, state, basis, loA, hiA, blockIdx.x * T::X, ty * T::Y, tz * T::Z, T::X, T::Y,
+                                T::Z, prim, pot);
 }
 
 template <typename real, int D>
@@ -107,30 +109,40 @@ __global__ void __launch_bounds__(kThreads) roeFluxXformKernel(Grid g, const dou
 
 template <typename real, bool GRAV>
 void launchRoeBasisG(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int loA, int hiA,
-                     const real* pot, cudaStream_t st) {
+                     const real* pot, cudaStream_t st, int slow0, int slowTiles) {
     auto grid = [&](int tx, int ty, int tz) {
         return dim3((unsigned)((g.S[0] + tx - 1) / tx), (unsigned)((g.S[1] + ty - 1) / ty),
                     (unsigned)((g.S[2] + tz - 1) / tz));
     };
-    if (g.dim == 1)
-        roeBasisKernel<real, 1, GRAV><<<grid(BasisTile<1>::X, 1, 1), 256, 0, st>>>(g, ph, state, basis, loA, hiA, pot);
-    else if (g.dim == 2)
-        roeBasisKernel<real, 2, GRAV><<<grid(BasisTile<2>::X, BasisTile<2>::Y, 1), 256, 0, st>>>(g, ph, state, basis,
-                                                                                                loA, hiA, pot);
+    if (g.dim == 1) {
+        roeBasisKernel<real, 1, GRAV><<<grid(BasisTile<1>::X, 1, 1), 256, 0, st>>>(g, ph, state, basis, loA, hiA, pot,
+                                                                                   0);
+        return;
+    }
+    dim3 gr = g.dim == 2 ? grid(BasisTile<2>::X, BasisTile<2>::Y, 1)
+                         : grid(BasisTile<3>::X, BasisTile<3>::Y, BasisTile<3>::Z);
+    unsigned& slow = g.dim == 2 ? gr.y : gr.z;
+    if (slow0 < 0) slow0 = 0;
+    if (slowTiles < 0 || slow0 + slowTiles > (int)slow) slowTiles = (int)slow - slow0;
+    if (slowTiles <= 0) return;
+    slow = (unsigned)slowTiles;
+    if (g.dim == 2)
+        roeBasisKernel<real, 2, GRAV><<<gr, 256, 0, st>>>(g, ph, state, basis, loA, hiA, pot, slow0);
     else
-        roeBasisKernel<real, 3, GRAV><<<grid(BasisTile<3>::X, BasisTile<3>::Y, BasisTile<3>::Z), 256, 0, st>>>(
-            g, ph, state, basis, loA, hiA, pot);
+        roeBasisKernel<real, 3, GRAV><<<gr, 256, 0, st>>>(g, ph, state, basis, loA, hiA, pot, slow0);
 }
 
 // REF: faces along [2, S-2] (res/EulerRoe.cl:27-34, res/Roe.cl:88-95); SEAM: [1, S-1].
 // pot: the gravitational potential, or null for a zero potential.
 template <typename real>
 void launchRoeBasis(const Grid& g, const Phys<real>& ph, const real* state, real* basis, int seam, cudaStream_t st,
-                    const real* pot) {
+                    const real* pot, int slow0, int slowTiles) {
     int loA = seam ? 1 : 2, hiA = seam ? 0 : 1;
-    if (pot) launchRoeBasisG<real, true>(g, ph, state, basis, loA, hiA, pot, st);
-    else launchRoeBasisG<real, false>(g, ph, state, basis, loA, hiA, nullptr, st);
+    if (pot) launchRoeBasisG<real, true>(g, ph, state, basis, loA, hiA, pot, st, slow0, slowTiles);
+    else launchRoeBasisG<real, false>(g, ph, state, basis, loA, hiA, nullptr, st, slow0, slowTiles);
 }
+
+int roeBasisSlowTile(int dim) { return dim == 2 ? BasisTile<2>::Y : dim == 3 ? BasisTile<3>::Z : 1; }
 
 template <typename real>
 void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigned long long* acc, unsigned* health,
@@ -196,7 +208,7 @@ void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* ba
 
 #define INST(real)                                                                                              \
     template void launchRoeBasis<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t,    \
-                                       const real*);                                                            \
+                                       const real*, int, int);                                                  \
     template void launchRoeDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                     cudaStream_t);                                                             \
     template void launchRoeDeltaQ<real>(const Grid&, const real*, const real*, real*, int, cudaStream_t);       \
