@@ -287,10 +287,12 @@ def batched_sweep(hg, _abi, ic, args):
     }
 
 
-def smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, pert, ndir=8):
+def smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, loss_difference, pert, ndir=8, eps_list=(1e-6, 1e-5, 1e-4)):
     """The same gradient check on a configuration where the rollout is differentiable:
     a smooth periodic flow with velocities away from zero (no face switches its upwind
-    side) and the smooth VanAlbada1 limiter, 512^2, RK2, the same step count."""
+    side) and the smooth VanAlbada1 limiter, 512^2, RK2, the same step count; central
+    differences at each step size of `eps_list` (at 1e-6 the rounding of the two
+    200-step trajectories is a visible part of the difference quotient)."""
     import torch
     f = [ic.smooth_perturbation((n, n), seed=400 + k, amp=1.)[0] for k in range(4)]
     u0 = ic.build_state_euler(2, 1.4, 1. + .2 * f[0], .4 + .05 * f[1], .3 + .05 * f[2], 0.,
@@ -312,24 +314,27 @@ def smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, pert, ndir=8):
     s_.synchronize()
     gh = g.cpu().numpy()
     rng = np.random.default_rng(300)
-    errs = []
+    dirs = []
     for _ in range(ndir):
         d = rng.standard_normal(u0.size)
-        d /= np.linalg.norm(d)
-        vals = []
-        for sgn in (1, -1):
-            s_.resetState(u0 + sgn * 1e-6 * d)
-            s_.update_frozen_dt(dts)
-            vals.append(loss_and_cotangent(s_.getState(), target)[0])
-        errs.append(((vals[0] - vals[1]) / 2e-6, float(np.dot(gh, d))))
+        dirs.append(d / np.linalg.norm(d))
+    out = {"workload": "smooth drifting flow 512^2, VanAlbada1, RK2, %d steps" % args.adjoint_steps}
+    for eps in eps_list:
+        errs = []
+        for d in dirs:
+            ends = []
+            for sgn in (1, -1):
+                s_.resetState(u0 + sgn * eps * d)
+                s_.update_frozen_dt(dts)
+                ends.append(s_.getState().copy())
+            errs.append((loss_difference(ends[0], ends[1], target) / (2 * eps), float(np.dot(gh, d))))
+        out["eps_%g" % eps] = fd_stats(errs, eps)
     cp.close()
     s_.close()
-    out = fd_stats(errs)
-    out["workload"] = "smooth drifting flow 512^2, VanAlbada1, RK2, %d steps" % args.adjoint_steps
     return out
 
 
-def fd_stats(pairs):
+def fd_stats(pairs, eps):
     """(finite difference, adjoint) directional derivatives along unit random directions:
     each error is |fd - ad| over the RMS of ad across the directions (a direction nearly
     orthogonal to the gradient has ad ~ 0 and no meaningful relative error of its own)."""
@@ -337,7 +342,7 @@ def fd_stats(pairs):
     ad = np.array([p[1] for p in pairs])
     scale = float(np.sqrt(np.mean(ad ** 2)))
     err = np.abs(fd - ad) / scale
-    return {"directions": len(pairs), "eps": 1e-6, "rms_directional_derivative": scale,
+    return {"directions": len(pairs), "eps": eps, "rms_directional_derivative": scale,
             "rel_err_median": float(np.median(err)), "rel_err_max": float(err.max()),
             "within_1e-6": int((err <= 1e-6).sum())}
 
@@ -417,7 +422,8 @@ def adjoint_measure(hg, _abi, ic, args):
     recompute + reverse steps.  Loss = mean over interior cells of
     (rho_T - rho_target)^2 with rho_target = rho_T + a smooth 1e-2 perturbation
     (seed 200).  Central differences (eps 1e-6, unit random directions, seed 300) of
-    the frozen-dt forward check the gradient of problem 0."""
+    the frozen-dt forward check the gradient of problem 0; the loss difference is formed
+    cell by cell (loss_difference)."""
     import torch
     n = 512
     shape = (n, n, N_STATES)
@@ -431,6 +437,14 @@ def adjoint_measure(hg, _abi, ic, args):
         lam = np.zeros(shape)
         lam[..., 0][mask] = 2 * r[mask] / cnt
         return float(np.sum(r[mask] ** 2) / cnt), lam.reshape(-1)
+
+    def loss_difference(ua, ub, target):
+        """loss(ua) - loss(ub) formed cell by cell, (a - b)(a + b - 2 target): the
+        difference of the two sums would lose it to their rounding (the loss is
+        ~1e-4, a difference across 2e-6 of a unit direction ~1e-14)."""
+        a = ua.reshape(shape)[..., 0][mask]
+        b = ub.reshape(shape)[..., 0][mask]
+        return float(np.sum((a - b) * (a + b - 2 * target[mask])) / mask.sum())
 
     fwd_ms = bwd_ms = plain_ms = 0.
     fd = None
@@ -466,20 +480,21 @@ def adjoint_measure(hg, _abi, ic, args):
             for _ in range(args.fd_directions):
                 d = rng.standard_normal(u0.size)
                 d /= np.linalg.norm(d)
-                vals = []
+                ends = []
                 for sgn in (1, -1):
                     s_.resetState(u0 + sgn * 1e-6 * d)
                     s_.update_frozen_dt(dts)
-                    vals.append(loss_and_cotangent(s_.getState(), target)[0])
-                fdv = (vals[0] - vals[1]) / 2e-6
+                    ends.append(s_.getState().copy())
+                fdv = loss_difference(ends[0], ends[1], target) / 2e-6
                 errs.append((fdv, float(np.dot(gh, d))))
-            fd = fd_stats(errs)
+            fd = fd_stats(errs, 1e-6)
             fd.update({
                   "note": "MinMod and the upwind choice have kinks; on this noisy state perturbations cross "
                           "some of them, so a difference quotient is not a derivative everywhere"})
         cp.close()
         s_.close()
-    fd_smooth = smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, pert) if args.fd_directions > 0 else None
+    fd_smooth = (smooth_fd(hg, _abi, ic, args, n, loss_and_cotangent, loss_difference, pert)
+                 if args.fd_directions > 0 else None)
     steps_total = args.adjoint_steps * args.adjoint_problems
     return {
         "workload": "%d x KH 512^2 (seeds 100..), EulerRoe RK2 MinMod FP64, %d steps, checkpoints every 20"
