@@ -495,15 +495,16 @@ bool Solver<real>::hostPipelined() const {
 }
 
 // One update() whose state comes from host memory `in` (upload) and/or goes back to
-// host memory `out` (download), with the copies overlapped with the step's own work.
+// host memory `out` (download), with the copies overlapped with the step's own work
+// (EulerRoe: the eigenbasis; EulerHLLC / EulerHLL: the wave speeds).
 // The slowest axis (y in 2D, z in 3D) is cut into bands of slow-axis tiles.  Upload:
 // band after band goes up on the copy stream, the last band first (it holds the planes
 // the periodic / mirror / free-flow fill of the first ghost planes reads), then band
 // 0, 1, ...; the solver's stream takes each band as it lands: E += 0 (the zero
 // potential's resetState pass), the ghost fill of the other axes on the band's planes,
-// then the band's share of the eigenbasis, which reads the band's planes and the one
-// below.  The slow axis's own ghost fill runs once the first and last bands are in,
-// before the first band's eigenbasis.  Download: the last stage's combine runs band
+// then the band's share of the eigenbasis (or wave speeds), which reads the band's
+// planes and the one below.  The slow axis's own ghost fill runs once the first and
+// last bands are in, before the first band's share.  Download: the last stage's combine runs band
 // by band and each band goes down as soon as it is written.  Every cell sees the same
 // operations as in set_state + update + get_state, so the results are the same bits.
 template <typename real>
@@ -728,6 +729,20 @@ void HLL<real>::initStep() {                                 // HLL::initStep (H
     this->launch("hllc_wave_speeds", 1, [&] {
         launchHllcWaves<real>(this->rc.grid, this->ph, this->state.template as<real>(), waves.template as<real>(),
                               this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream, this->livePotential());
+    });
+}
+
+// the wave speeds of the faces of the band's cells (they read the band's planes and
+// the plane below the band)
+template <typename real>
+void HLL<real>::bandedPrologueWork(int tile0, int tiles) {
+    const Grid& g = this->rc.grid;
+    const int T_A = this->slowTile();
+    const long long S_A = g.S[this->rc.dim - 1], plane = (long long)g.V / S_A;
+    const long long p0 = (long long)tile0 * T_A, p1 = std::min<long long>((long long)(tile0 + tiles) * T_A, S_A);
+    this->launch("hllc_wave_speeds", 1, [&] {
+        launchHllcWaves<real>(g, this->ph, this->state.template as<real>(), waves.template as<real>(),
+                              this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream, nullptr, p0 * plane, p1 * plane);
     });
 }
 

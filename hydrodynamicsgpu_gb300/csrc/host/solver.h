@@ -317,6 +317,11 @@ protected:
     void initStep() override;                     // calcEigenvalues (frozen for the step)
     void calcTimestep() override;
     void step() override;
+    // bands of the wave speeds: the same plane granularity as the Roe eigenbasis bands
+    bool bandedPrologue() const override { return !this->livePotential(); }
+    int slowTile() const override { return roeBasisSlowTile(this->rc.dim); }
+    void bandedPrologueWork(int tile0, int tiles) override;
+    void bandedPrologueEnd() override { calcTimestep(); }
 };
 
 template <typename real>

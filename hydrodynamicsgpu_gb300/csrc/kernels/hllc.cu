@@ -23,9 +23,9 @@ inline unsigned blocksFor(long long n) { return (unsigned)((n + kThreads - 1) / 
 template <typename real, int D, bool HLL, bool GRAV>
 __global__ void __launch_bounds__(kThreads) hllcWaveKernel(Grid g, Phys<real> ph, double gq,
                                                            const real* __restrict__ state, real* __restrict__ waves,
-                                                           const real* __restrict__ pot) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                           const real* __restrict__ pot, long long c0, long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     hllcWaveCell<real, D, HLL, GRAV>(g, ph, gq, state, waves, c, x, y, z, pot);
@@ -63,10 +63,14 @@ __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph
 // pot: the gravitational potential, or null for a zero potential
 template <typename real, bool GRAV>
 void launchHllcWavesG(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st,
-                      const real* pot) {
+                      const real* pot, long long c0, long long c1) {
+    if (c1 < 0 || c1 > g.V) c1 = g.V;
+    if (c0 < 0) c0 = 0;
+    if (c0 >= c1) return;
     // (gamma + 1.) / (2. * gamma) is a per-program constant (double literals); computed once, identically
     double gq = ((double)ph.gamma + 1.) / (2. * (double)ph.gamma);
-#define L(DD, H) hllcWaveKernel<real, DD, H, GRAV><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, gq, state, waves, pot)
+#define L(DD, H) \
+    hllcWaveKernel<real, DD, H, GRAV><<<blocksFor(c1 - c0), kThreads, 0, st>>>(g, ph, gq, state, waves, pot, c0, c1)
     if (hll) {
         if (g.dim == 1) L(1, true);
         else if (g.dim == 2) L(2, true);
@@ -81,9 +85,9 @@ void launchHllcWavesG(const Grid& g, const Phys<real>& ph, const real* state, re
 
 template <typename real>
 void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st,
-                     const real* pot) {
-    if (pot) launchHllcWavesG<real, true>(g, ph, state, waves, hll, st, pot);
-    else launchHllcWavesG<real, false>(g, ph, state, waves, hll, st, nullptr);
+                     const real* pot, long long c0, long long c1) {
+    if (pot) launchHllcWavesG<real, true>(g, ph, state, waves, hll, st, pot, c0, c1);
+    else launchHllcWavesG<real, false>(g, ph, state, waves, hll, st, nullptr, c0, c1);
 }
 
 template <typename real>
@@ -120,7 +124,7 @@ void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, cons
 
 #define INST(real)                                                                                                \
     template void launchHllcWaves<real>(const Grid&, const Phys<real>&, const real*, real*, int, cudaStream_t,    \
-                                        const real*);                                                             \
+                                        const real*, long long, long long);                                       \
     template void launchHllcDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                      cudaStream_t);                                                               \
     template void launchHllcFlux<real>(const Grid&, const Phys<real>&, const real*, const real*, real*, unsigned*, \

@@ -77,9 +77,10 @@ void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* ba
 int roeRecordSize(int dim);
 
 // ---- hllc.cu ----
+// the wave speeds of the faces of cells [c0, c1) (default: every cell)
 template <typename real>
 void launchHllcWaves(const Grid& g, const Phys<real>& ph, const real* state, real* waves, int hll, cudaStream_t st,
-                     const real* pot = nullptr);
+                     const real* pot = nullptr, long long c0 = 0, long long c1 = -1);
 template <typename real>
 void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsigned long long* acc, unsigned* health,
                   cudaStream_t st);

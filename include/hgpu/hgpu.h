@@ -199,19 +199,21 @@ int hgpu_get_state(hgpu_solver* s, void* host_state, size_t count);
  * non-NULL, after it finished, with that step's dt.  */
 int hgpu_update(hgpu_solver* s, int nsteps, double* last_dt);
 
+/* The same call under the name a step-oriented binding uses. */
+int hgpu_step(hgpu_solver* s, int nsteps, double* last_dt);
+
 /* Upload, advance, download in one call: host_in -> Converter::toGPU + resetState
  * (Solver.cpp:333-337, as hgpu_set_state), nsteps x Solver::update (as hgpu_update),
  * then Converter::fromGPU (Solver.cpp:339-342) into host_out, with the same bits as
- * those three calls.  In 2D and 3D EulerRoe without a fixed dt, gravity or a static
+ * those three calls.  In 2D and 3D without a fixed dt, gravity or a static
  * potential, the copies are cut into bands along the slowest axis and overlapped
- * with the first step's ghost fill and eigenbasis and with the last step's final
- * combine; page-locked host buffers let them run asynchronously.  host_in and
- * host_out (in_count = out_count = the state's element count) may be the same
- * buffer.  Returns after the download, with the last step's dt in last_dt. */
+ * with the first step's ghost fill and eigenbasis (EulerRoe) or wave speeds
+ * (EulerHLLC, EulerHLL) and with the last step's final combine; page-locked host
+ * buffers let them run asynchronously.  host_in and host_out (in_count = out_count
+ * = the state's element count) may be the same buffer.  Returns after the download,
+ * with the last step's dt in last_dt. */
 int hgpu_update_host(hgpu_solver* s, const void* host_in, size_t in_count, int nsteps, void* host_out,
                      size_t out_count, double* last_dt);
-/* The same call under the name a step-oriented binding uses. */
-int hgpu_step(hgpu_solver* s, int nsteps, double* last_dt);
 
 /* dt of the most recent step (blocks on the solver's stream). */
 int hgpu_last_dt(hgpu_solver* s, double* dt);

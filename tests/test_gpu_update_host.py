@@ -2,9 +2,10 @@
 bands overlapped with the first and last step) against hgpu_set_state +
 hgpu_update + hgpu_get_state on the same input: the same bits, state and dt.
 
-The overlapped form covers 2D/3D EulerRoe; the band count depends on the size along
-the slowest axis (one band below 128 rows in 2D / 16 planes in 3D), so the sizes
-below take 1, 2, 4 and 16 bands.  The other configurations take the plain form."""
+The overlapped form covers 2D/3D EulerRoe, EulerHLLC and EulerHLL without a fixed dt,
+gravity or a static potential; the band count depends on the size along the slowest
+axis (one band below 128 rows in 2D / 16 planes in 3D), so the sizes below take 1, 2,
+4 and 16 bands.  The other configurations take the plain form."""
 import numpy as np
 import pytest
 
@@ -51,9 +52,9 @@ def check(hg, cfg, init, nsteps=1, pinned=False):
         s.close()
 
 
-@pytest.mark.parametrize("nsteps", [1, 3])
-def test_kh_2048_roe_rk4(hg, nsteps):
-    cfg = _abi.make_config(solver="EulerRoe", size=(2048, 2048), boundary="PERIODIC", limiter="MinMod",
+@pytest.mark.parametrize("solver,nsteps", [("EulerRoe", 1), ("EulerRoe", 3), ("EulerHLLC", 2)])
+def test_kh_2048_rk4(hg, solver, nsteps):
+    cfg = _abi.make_config(solver=solver, size=(2048, 2048), boundary="PERIODIC", limiter="MinMod",
                            integrator="RungeKutta4")
     check(hg, cfg, ic.kelvin_helmholtz(size=(2048, 2048), seed=0).reshape(-1), nsteps, pinned=True)
 
@@ -85,14 +86,28 @@ def test_roe_3d(hg, size, bnd, integ):
     check(hg, cfg, random_state(cfg, seed=8), nsteps=2)
 
 
+@pytest.mark.parametrize("solver,size,bnd,integ,prec", [
+    ("EulerHLLC", (20, 18), "PERIODIC", "RungeKutta4", _abi.FP64),           # 1 band
+    ("EulerHLLC", (64, 520), "MIRROR", "RungeKutta2", _abi.FP64),            # 4 bands
+    ("EulerHLL", (40, 300), "FREEFLOW", "RungeKutta3TVD", _abi.FP64),        # 2 bands, alpha 3/4
+    ("EulerHLLC", (33, 517), "PERIODIC", "ForwardEuler", _abi.FP32),         # 4 bands, FE, FP32
+    ("EulerHLL", (10, 9, 40), "MIRROR", "RungeKutta2", _abi.FP64),           # 3D, 2 bands
+    ("EulerHLLC", (12, 11, 70), "PERIODIC", "RungeKutta4", _abi.FP64),       # 3D, 4 bands
+])
+def test_hll_family(hg, solver, size, bnd, integ, prec):
+    cfg = _abi.make_config(solver=solver, size=size, boundary=bnd, integrator=integ, limiter="MinMod",
+                           precision=prec)
+    check(hg, cfg, random_state(cfg, seed=13, blocky=True), nsteps=2)
+
+
 def test_mixed_boundaries_per_side(hg):
     bnd = [("PERIODIC", "PERIODIC"), ("MIRROR", "FREEFLOW")]
     cfg = _abi.make_config(solver="EulerRoe", size=(30, 290), boundary=bnd, integrator="RungeKutta4")
     check(hg, cfg, random_state(cfg, seed=9), nsteps=2)
 
 
-@pytest.mark.parametrize("kw", [dict(solver="EulerHLLC", size=(40, 300)),
-                                dict(solver="EulerHLL", size=(12, 11, 40)),
+@pytest.mark.parametrize("kw", [dict(solver="EulerHLLC", size=(300,)),
+                                dict(solver="EulerHLLC", size=(40, 300), use_fixed_dt=True, fixed_dt=1e-4),
                                 dict(solver="EulerRoe", size=(300,)),
                                 dict(solver="EulerRoe", size=(40, 300), use_fixed_dt=True, fixed_dt=1e-4),
                                 dict(solver="EulerRoe", size=(40, 300), use_gravity=True,
