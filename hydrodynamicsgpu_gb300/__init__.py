@@ -23,6 +23,8 @@ _P = ctypes.c_void_p
 _CFG = ctypes.POINTER(HgpuConfig)
 SIGNATURES = {
     "hgpu_config_default": (ctypes.c_int, [_CFG]),
+    "hgpu_config_from_file": (ctypes.c_int, [ctypes.c_char_p, _CFG]),
+    "hgpu_config_from_string": (ctypes.c_int, [ctypes.c_char_p, _CFG]),
     "hgpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "hgpu_last_error": (ctypes.c_char_p, []),
     "hgpu_create": (ctypes.c_int, [_CFG, ctypes.POINTER(_P)]),
@@ -83,6 +85,20 @@ SIGNATURES = {
 
 class KernelTime(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
+
+
+def config_from_file(path):
+    """An HgpuConfig read from a config.lua-style settings file (hgpu_config_from_file)."""
+    cfg = HgpuConfig()
+    check(lib().hgpu_config_from_file(os.fsencode(path), ctypes.byref(cfg)))
+    return cfg
+
+
+def config_from_string(text):
+    """An HgpuConfig read from the text of a config.lua-style settings file."""
+    cfg = HgpuConfig()
+    check(lib().hgpu_config_from_string(text.encode(), ctypes.byref(cfg)))
+    return cfg
 
 
 def select_device(device):

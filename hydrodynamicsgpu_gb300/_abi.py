@@ -14,6 +14,7 @@ STATUS_NAMES = {
     4: "HGPU_ERR_TIMEOUT", 5: "HGPU_ERR_OOB", 6: "HGPU_ERR_ARG", 7: "HGPU_ERR_UNSUPPORTED",
     8: "HGPU_ERR_NOMEM",
 }
+(OK, ERR_CONFIG, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_OOB, ERR_ARG, ERR_UNSUPPORTED, ERR_NOMEM) = range(9)
 
 SOLVERS = {"EulerRoe": 0, "EulerHLLC": 1, "EulerHLL": 2}
 BOUNDARIES = {"NONE": -1, "PERIODIC": 0, "MIRROR": 1, "FREEFLOW": 2}

@@ -36,6 +36,7 @@ SOURCES = {
     "host/batch_solver.cu": [],
     "host/solver.cu": [],
     "host/capi.cu": [],
+    "host/config_file.cu": [],
 }
 HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
            "kernels/combine_cells.cuh", "kernels/batch.h", "kernels/batch_common.cuh", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",

@@ -131,23 +131,72 @@ def configuration(n, size=(256, 256), gamma=1.4, dtype=np.float64):
     return quadrant(size, CONFIGURATIONS[n], gamma=gamma, dtype=dtype)
 
 
+def _exp_basic(x):
+    """exp(x) from basic IEEE operations only (add, multiply, divide, scaling by 2^n), so
+    that the same inputs give the same bits on every platform (libm and vectorised
+    numpy exponentials differ between machines in the last bit).  Cody-Waite range
+    reduction x = n ln2 + r, |r| <= ln2 / 2, with ln2 split into a 32-bit head and a
+    tail, then the Taylor series of exp(r) to degree 18 by Horner's rule (truncation
+    below 1e-22 relative), scaled by 2^n."""
+    x = np.asarray(x, dtype=np.float64)
+    ln2_hi = 0.693147180369123816490     # ln 2 rounded to 32 significant bits
+    ln2_lo = 1.90821492927058770002e-10  # ln 2 - ln2_hi
+    n = np.rint(x / 0.6931471805599453)
+    r = (x - n * ln2_hi) - n * ln2_lo
+    p = np.ones_like(r)
+    for k in range(18, 0, -1):
+        p = 1.0 + p * r / float(k)
+    return np.ldexp(p, n.astype(np.int64))
+
+
+def _box_periodic(a, axis, width):
+    """Periodic moving average of odd `width` along `axis`: the first window summed
+    term by term, each next one by adding the entering and subtracting the leaving
+    plane, in a fixed order."""
+    h = width // 2
+    b = np.moveaxis(a, axis, 0)
+    n = b.shape[0]
+    out = np.empty_like(b)
+    acc = np.zeros_like(b[0])
+    for k in range(-h, h + 1):
+        acc = acc + b[k % n]
+    out[0] = acc
+    for i in range(1, n):
+        acc = (acc + b[(i + h) % n]) - b[(i - 1 - h) % n]
+        out[i] = acc
+    return np.moveaxis(out / float(width), 0, axis)
+
+
+def _fsum(a):
+    """Exactly rounded sum of an array (math.fsum over chunks of partial sums is not
+    exact, so the values themselves are passed)."""
+    return math.fsum(np.ravel(a).tolist())
+
+
 def lognormal_grf(size=(256, 256, 256), xmin=(0., 0., 0.), xmax=(1., 1., 1.), gamma=5. / 3., sigma=.5,
                   corr_cells=16.0, seed=1, dtype=np.float64):
     """3D benchmark: density exp(sigma*G) normalised to mean 1, where G is a
-    unit-variance Gaussian random field with a Gaussian correlation of
-    `corr_cells` cells (white noise filtered in Fourier space, seeded); p=1, u=0."""
+    unit-variance Gaussian random field with a correlation length of `corr_cells`
+    cells; p=1, u=0.  G is seeded white noise (uniform, unit variance) smoothed on the
+    periodic grid by three passes of a moving average per axis, whose product is a
+    near-Gaussian kernel of standard deviation sqrt((w^2 - 1)/4) ~ corr_cells cells
+    (w odd), then centred and scaled to unit variance with exactly rounded sums.
+    Only basic IEEE operations in a fixed order are used (see _exp_basic), so a seed
+    gives the same state, bit for bit, on every platform."""
     nz, ny, nx = size[2], size[1], size[0]
     rng = np.random.default_rng(seed)
-    white = rng.standard_normal((nz, ny, nx))
-    kz = np.fft.fftfreq(nz)[:, None, None]
-    ky = np.fft.fftfreq(ny)[None, :, None]
-    kx = np.fft.rfftfreq(nx)[None, None, :]
-    k2 = (2 * math.pi) ** 2 * (kx * kx + ky * ky + kz * kz)
-    filt = np.exp(-.5 * k2 * corr_cells * corr_cells)
-    g = np.fft.irfftn(np.fft.rfftn(white) * filt, s=(nz, ny, nx), axes=(0, 1, 2))
-    g = (g - g.mean()) / g.std()
-    rho = np.exp(sigma * g)
-    rho = rho / rho.mean()
+    s3 = math.sqrt(3.0)
+    g = rng.uniform(-s3, s3, (nz, ny, nx))
+    width = int(round(math.sqrt(4. * corr_cells * corr_cells + 1.)))
+    width += 1 - width % 2
+    for axis in (0, 1, 2):
+        for _ in range(3):
+            g = _box_periodic(g, axis, width)
+    count = float(g.size)
+    g = g - _fsum(g) / count
+    g = g / math.sqrt(_fsum(g * g) / count)
+    rho = _exp_basic(sigma * g)
+    rho = rho / (_fsum(rho) / count)
     return build_state_euler(3, gamma, rho, 0.0, 0.0, 0.0, 1.0, dtype)
 
 

@@ -151,6 +151,24 @@ typedef struct hgpu_solver hgpu_solver;  /* opaque handle */
  * Solver.cpp:196 ForwardEuler) for a 2D 256x256 EulerRoe run. */
 int hgpu_config_default(hgpu_config* cfg);
 
+/* Fill *cfg from a config.lua-style settings file: replaces the Lua configuration
+ * the reference host reads through LuaCxx (src/HydroGPUApp.cpp:157-208, :330;
+ * src/Solver/Solver.cpp:196-197, 285-307; res/config.lua:26-94).  The file holds
+ * assignments of literal values (numbers with arithmetic, strings, booleans,
+ * tables, reads of names assigned earlier); keys read: solverName, integratorName,
+ * slopeLimiter (not slopeLimiterName, which the reference never reads), size,
+ * xmin, xmax, boundaryMethods, cfl, useFixedDT, fixedDT, useGravity,
+ * gaussSeidelMaxIter, defs.idealGas_heatCapacityRatio and
+ * defs.selfGrav_gravitationalConstant; absent keys keep hgpu_config_default's
+ * values.  Statements that need a Lua interpreter (require, function calls, if,
+ * function definitions) are refused with HGPU_ERR_CONFIG and their line number
+ * (hgpu_last_error); a missing solverName (the reference default EulerBurgers) or
+ * BackwardEulerConjugateGradient with HGPU_ERR_UNSUPPORTED.  *cfg is written only
+ * on success. */
+int hgpu_config_from_file(const char* path, hgpu_config* cfg);
+/* The same from the text of such a file. */
+int hgpu_config_from_string(const char* text, hgpu_config* cfg);
+
 /* Human-readable name of a status code. */
 const char* hgpu_status_string(int status);
 

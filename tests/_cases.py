@@ -31,6 +31,22 @@ def same(a, b):
     return np.array_equal(a, b, equal_nan=True)
 
 
+def canonical(a):
+    """A copy of `a` under the parity rule's equivalence: -0 mapped to +0 and every NaN
+    to the one quiet-NaN pattern, so that equal states under `same` give equal bytes."""
+    c = np.array(a, copy=True)
+    c[c == 0] = 0
+    c[np.isnan(c)] = np.nan
+    return c
+
+
+def state_digest(a):
+    """SHA-256 of the canonical bytes of a state (little-endian, native element type)."""
+    import hashlib
+    c = canonical(np.asarray(a).reshape(-1))
+    return hashlib.sha256(c.astype(c.dtype.newbyteorder("<"), copy=False).tobytes()).hexdigest()
+
+
 def describe_diff(a, b):
     a64, b64 = a.astype(np.float64), b.astype(np.float64)
     bad = ~((a64 == b64) | (np.isnan(a64) & np.isnan(b64)))
