@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity measurement")
     ap.add_argument("--gravity-size", type=int, default=2048)
+    ap.add_argument("--gravity-detail", action="store_true", help="per-kernel breakdown of the self-gravity step")
     ap.add_argument("--batch-problems", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--adjoint-problems", type=int, default=16)
@@ -412,7 +413,8 @@ def gravity_measure(hg, _abi, ic, args):
     return {"workload": "self-gravitating blobs %dx%d, EulerRoe FP64 RK4 MinMod periodic, useGravity, "
                         "gaussSeidelMaxIter 20, G 1" % (n, n),
             "value": interior / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "kernels_per_step": kps,
-            "reset_s": reset_s, "relax_sweep": sweep, "kernels": breakdown, "health_flags": health}
+            "reset_s": reset_s, "relax_sweep": sweep, "health_flags": health,
+            "kernels": breakdown if args.gravity_detail else None}
 
 
 def adjoint_measure(hg, _abi, ic, args):
@@ -507,12 +509,55 @@ def adjoint_measure(hg, _abi, ic, args):
     }
 
 
-# DRAM bytes (read + write) per interior cell of one launch, from the ncu captures in
-# profiles/kernels_kh1024.md (KH 1024x1024, same kernels); traffic grows with the cells
-# processed, so the bench workload's per-launch traffic is this times its interior cells.
-# roe_flux is its two passes together (corrections 148 B + transforms 420 B).
+# DRAM bytes (read + write) per interior cell of one launch, from ncu captures of the
+# same kernels on KH 1024x1024 (dram__bytes_read.sum + dram__bytes_write.sum over the
+# interior cells); traffic grows with the cells processed, so the bench workload's
+# per-launch traffic is this times its interior cells.  roe_flux is its two passes
+# together (corrections 148 B + transforms 420 B).
 MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 568.0, "roe_delta_q_tilde": 252.0, "roe_eigenbasis": 245.0,
                              "flux_divergence_combine": 123.0}
+
+# Instructions the FP64 unit executes per interior cell of one launch of each kernel of
+# the EulerRoe FP64 step (MinMod), from ncu's smsp__inst_executed_pipe_fp64 (warp
+# instructions x 32) over the cells of a KH 512x512 step of the same kernels; roe_flux
+# is its two passes together (corrections 30.6 + transforms 65.5).
+FP64_PIPE_PER_CELL = {"roe_eigenbasis": 71.4, "cfl_min_reduce": 9.9, "roe_delta_q_tilde": 37.7,
+                      "roe_flux": 96.1, "flux_divergence_combine": 40.9, "state_check": 7.0}
+
+
+def fp64_roofline(prof, value, fp64_peak):
+    """The step's binding roofline: FP64-unit instructions per cell-update (the table
+    above times each kernel's launches per step, from a profile of `steps` steps)
+    times cell-updates/s, against the FP64 unit's issue rate measured in this run
+    (hgpu_fp64_peak, FMA instructions per second on all SMs)."""
+    steps = prof["roe_eigenbasis"][0] if "roe_eigenbasis" in prof else 1
+    per_update = sum(FP64_PIPE_PER_CELL.get(k, 0.) * v[0] / steps for k, v in prof.items())
+    achieved = per_update * value
+    return per_update, achieved, achieved / fp64_peak
+
+
+def summary_block(value, e2e, roofline, batched, adjoint):
+    """The headline numbers in a few keys, placed last in the JSON line."""
+    out = {"value": value, "e2e": e2e["value"] if e2e else None,
+           "fp64_frac": roofline["frac"], "hbm_frac_dominant_kernel": roofline["hbm"]["frac"],
+           "hbm_frac_step": roofline["hbm_step"]["frac"]}
+    if batched:
+        out["batched_ms_per_step"] = batched["batched"]["ms_per_step"]
+        out["plain_sequential_ms_per_step"] = batched["plain_sequential"]["ms_per_step"]
+        out["plain_interleaved_ms_per_step"] = batched["plain_interleaved"]["ms_per_step"]
+        out["batched_speedup_vs_plain_sequential"] = batched["speedup_vs_plain_sequential"]
+        out["batched_speedup_vs_plain_interleaved"] = batched["speedup_vs_plain_interleaved"]
+    if adjoint:
+        out["adjoint_over_forward"] = adjoint["adjoint_over_forward"]
+        out["adjoint_over_plain_forward"] = adjoint["adjoint_over_plain_forward"]
+        fd = adjoint.get("finite_differences")
+        if fd:
+            out["fd_within_1e-6"] = "%d/%d" % (fd["within_1e-6"], fd["directions"])
+            out["fd_rel_err_median"] = fd["rel_err_median"]
+        fds = (adjoint.get("finite_differences_differentiable") or {}).get("eps_1e-06")
+        if fds:
+            out["fd_differentiable_within_1e-6"] = "%d/%d" % (fds["within_1e-6"], fds["directions"])
+    return out
 
 
 def run_gb300(args):
@@ -566,13 +611,21 @@ def run_gb300(args):
     achieved_gbs = bytes_per_launch / (dom_ms * 1e-3) / 1e9
     fp64_peak = hg.fp64_peak()
     traffic = MEASURED_TRAFFIC_PER_CELL.get(dom_name)
-    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind,
-                "traffic": traffic * interior if traffic else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 1024^2 "
-                                  "(profiles/kernels_kh1024.md), scaled by interior cells",
-                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": dom_ms,
-                "note": "compute-bound (FP64 unit + integer pipes carrying binary64 products), not HBM-bound; see fp64"}
+    per_update, fp64_achieved, fp64_frac = fp64_roofline(prof, value / world, fp64_peak)
+    step_bytes = 17 * N_STATES * 8          # compulsory bytes of an RK4 cell-update (17 state arrays)
+    step_gbs = step_bytes * value / world / 1e9
+    roofline = {"bound": "fp64", "kernel": "the whole step (each of its kernels is FP64-issue-bound)",
+                "achieved": fp64_achieved, "peak": fp64_peak, "unit": "FP64-unit instructions/s",
+                "frac": fp64_frac, "peak_source": "hgpu_fp64_peak measured in this run (FMA issue rate, all SMs)",
+                "fp64_inst_per_cell_update": per_update,
+                "traffic": traffic * interior if traffic else None, "traffic_kernel": dom_name,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per interior cell at 1024^2, "
+                                  "scaled by interior cells",
+                "hbm": {"kernel": dom_name, "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                        "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": dom_ms},
+                "hbm_step": {"bytes_per_cell_update": step_bytes, "achieved": step_gbs, "peak": peak_gbs,
+                             "unit": "GB/s", "frac": step_gbs / peak_gbs}}
     breakdown = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / sum(x[1] for x in prof.values())}
                  for k, v in prof.items()}
 
@@ -626,17 +679,17 @@ def run_gb300(args):
                    "interior_cells": interior, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (state 134 MB, eigenbasis 1.14 GB, fluxes 268 MB per step)"},
         "roofline": roofline,
-        "fp64": {"fma_per_s_peak_measured": fp64_peak, "bound": "fp64 issue"},
         "kernels": breakdown,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
         "fp32": fp32,
-        "batched_sweep": batched,
-        "adjoint": adjoint,
         "self_gravity": gravity,
+        "adjoint": adjoint,
+        "batched_sweep": batched,
         "gpu_launches": kernels_per_step * args.steps,
         "health_flags": health,
+        "summary": summary_block(value, e2e, roofline, batched, adjoint),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

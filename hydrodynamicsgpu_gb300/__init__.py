@@ -42,6 +42,7 @@ SIGNATURES = {
     "hgpu_last_dt": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_synchronize": (ctypes.c_int, [_P]),
     "hgpu_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "hgpu_set_health_mode": (ctypes.c_int, [_P, ctypes.c_int]),
     "hgpu_state_device_ptr": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "hgpu_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "hgpu_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
@@ -77,6 +78,7 @@ SIGNATURES = {
     "hgpu_batch_timed_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "hgpu_batch_dts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "hgpu_batch_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "hgpu_batch_problem_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int]),
     "hgpu_batch_get_tuning": (ctypes.c_int, [_P, _P]),
     "hgpu_batch_set_tuning": (ctypes.c_int, [_P, _P]),
     "hgpu_batch_autotune": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
@@ -283,6 +285,10 @@ class Solver:
     def synchronize(self):
         check(lib().hgpu_synchronize(self.h))
 
+    def set_health_mode(self, mode):
+        """_abi.HEALTH_OFF / HEALTH_RECORD (default) / HEALTH_STRICT (hgpu_set_health_mode)."""
+        check(lib().hgpu_set_health_mode(self.h, int(mode)))
+
     def health(self):
         f = ctypes.c_uint32()
         check(lib().hgpu_health(self.h, ctypes.byref(f)))
@@ -409,6 +415,13 @@ class Batch:
         f = ctypes.c_uint32()
         check(lib().hgpu_batch_health(self.h, ctypes.byref(f)))
         return f.value
+
+    def problem_health(self):
+        """Every problem's health bits since the last read (hgpu_batch_problem_health)."""
+        n = len(self.cfgs)
+        out = (ctypes.c_uint32 * n)()
+        check(lib().hgpu_batch_problem_health(self.h, out, n))
+        return np.array(out[:], dtype=np.uint32)
 
     def info(self):
         n, cells, k = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int()

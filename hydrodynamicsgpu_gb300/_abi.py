@@ -12,9 +12,14 @@ HGPU_OK = 0
 STATUS_NAMES = {
     0: "HGPU_OK", 1: "HGPU_ERR_CONFIG", 2: "HGPU_ERR_CUDA", 3: "HGPU_ERR_NONFINITE",
     4: "HGPU_ERR_TIMEOUT", 5: "HGPU_ERR_OOB", 6: "HGPU_ERR_ARG", 7: "HGPU_ERR_UNSUPPORTED",
-    8: "HGPU_ERR_NOMEM",
+    8: "HGPU_ERR_NOMEM", 9: "HGPU_ERR_UNPHYSICAL",
 }
-(OK, ERR_CONFIG, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_OOB, ERR_ARG, ERR_UNSUPPORTED, ERR_NOMEM) = range(9)
+(OK, ERR_CONFIG, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_OOB, ERR_ARG, ERR_UNSUPPORTED, ERR_NOMEM,
+ ERR_UNPHYSICAL) = range(10)
+# health word bits (hgpu_health) and modes (hgpu_set_health_mode)
+HEALTH_NONFINITE_DT, HEALTH_HLLC_NOBRANCH, HEALTH_STATE_NONFINITE, HEALTH_STATE_DENSITY, HEALTH_STATE_PRESSURE = \
+    1, 2, 4, 8, 16
+HEALTH_OFF, HEALTH_RECORD, HEALTH_STRICT = 0, 1, 2
 
 SOLVERS = {"EulerRoe": 0, "EulerHLLC": 1, "EulerHLL": 2}
 BOUNDARIES = {"NONE": -1, "PERIODIC": 0, "MIRROR": 1, "FREEFLOW": 2}

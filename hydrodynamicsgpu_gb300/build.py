@@ -31,6 +31,7 @@ SOURCES = {
     "kernels/roe_record.cu": ["--fmad=false"],
     "kernels/display.cu": ["--fmad=false"],
     "kernels/gravity.cu": ["--fmad=false"],
+    "kernels/health.cu": ["--fmad=false"],
     "host/fits.cu": [],
     "host/adjoint.cu": [],
     "host/batch_solver.cu": [],
@@ -41,7 +42,7 @@ SOURCES = {
 HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
            "kernels/combine_cells.cuh", "kernels/batch.h", "kernels/batch_common.cuh", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",
            "kernels/adjoint.h", "host/adjoint.h",
-           "kernels/limiter_dual.cuh", "host/fits.h", "kernels/gravity.h"]
+           "kernels/limiter_dual.cuh", "host/fits.h", "kernels/gravity.h", "kernels/health.cuh"]
 
 
 def nvcc():

@@ -88,6 +88,7 @@ BatchSolver<real>::BatchSolver(const std::vector<hgpu_config>& cfgs) {
                   "dt accumulators");
     }
     health_ = DeviceBuffer(sizeof(unsigned), true);
+    healthP_ = DeviceBuffer(sizeof(unsigned) * host_.size(), true);
     queues_ = DeviceBuffer(sizeof(unsigned) * kQueues, true);
     if (integ_ != HGPU_INTEGRATOR_FORWARD_EULER) {
         plans_ = buildStagePlans<real>(integ_);
@@ -200,6 +201,8 @@ void BatchSolver<real>::update() {                       // Solver::update for e
             ++launches_;
         }
     }
+    L.stateCheck(health, healthP_.as<unsigned>(), nextQ());
+    ++launches_;
 }
 
 // capture one step into a CUDA graph (capture records the launches, it runs nothing)
@@ -283,6 +286,14 @@ unsigned BatchSolver<real>::readHealth() {
     cudaCheck(cudaMemcpy(&f, health_.get(), sizeof f, cudaMemcpyDeviceToHost), "health");
     cudaCheck(cudaMemset(health_.get(), 0, sizeof f), "health clear");
     return f;
+}
+
+template <typename real>
+void BatchSolver<real>::readProblemHealth(unsigned* out, int n) {
+    if (n != (int)host_.size()) throw ConfigError(HGPU_ERR_ARG, "health array size mismatch");
+    cudaCheck(cudaStreamSynchronize(stream), "sync");
+    cudaCheck(cudaMemcpy(out, healthP_.get(), sizeof(unsigned) * host_.size(), cudaMemcpyDeviceToHost), "health");
+    cudaCheck(cudaMemset(healthP_.get(), 0, sizeof(unsigned) * host_.size()), "health clear");
 }
 
 // "hllc-2d-rk2-f64-p512-<fnv1a of the sizes>"

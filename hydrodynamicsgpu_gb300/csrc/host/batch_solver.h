@@ -18,6 +18,8 @@ public:
     virtual void getState(int p, void* host, size_t count) = 0;
     virtual void dts(double* out, int n) = 0;
     virtual unsigned readHealth() = 0;
+    // read and clear every problem's health word (n = number of problems)
+    virtual void readProblemHealth(unsigned* out, int n) = 0;
     virtual void setTuning(const BatchTuning& tu) = 0;
     virtual BatchTuning tuning() const = 0;
     virtual void autotune(const std::string& cachePath, int steps) = 0;
@@ -38,6 +40,7 @@ public:
     void getState(int p, void* host, size_t count) override;
     void dts(double* out, int n) override;
     unsigned readHealth() override;
+    void readProblemHealth(unsigned* out, int n) override;
     void setTuning(const BatchTuning& tu) override;
     BatchTuning tuning() const override { return tuning_; }
     void autotune(const std::string& cachePath, int steps) override;
@@ -53,7 +56,7 @@ private:
     bool hllc_ = false, alphaBinary_ = true;
     long long totalCells_ = 0;
     double tunedMs_ = 0;
-    DeviceBuffer state_, faces_, dq_, flux_, probs_, sc_, acc_, health_, queues_, tiles_;
+    DeviceBuffer state_, faces_, dq_, flux_, probs_, sc_, acc_, health_, healthP_, queues_, tiles_;
     std::vector<DeviceBuffer> work_;
     StagePlans<real> plans_;
     BatchTuning tuning_{};

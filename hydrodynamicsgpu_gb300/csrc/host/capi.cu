@@ -27,6 +27,7 @@ struct hgpu_solver {
     std::unique_ptr<hgpu::RoeAdjoint> adjoint;   // created on first use
     std::vector<hgpu_checkpoint*> checkpoints;   // live trajectories of this solver
     hgpu::DeviceBuffer display;                   // one float per cell, created on first use
+    int healthMode = HGPU_HEALTH_RECORD;
 };
 
 struct hgpu_checkpoint {
@@ -58,6 +59,20 @@ int guarded(F f) {
 }
 
 void runSteps(hgpu_solver* h, int nsteps);
+
+// Strict health mode: wait for the solver's stream, then map the health word's bits
+// (left set) to a status.
+int healthStatus(hgpu_solver* h) {
+    if (h->healthMode != HGPU_HEALTH_STRICT) return HGPU_OK;
+    hgpu::cudaCheck(cudaStreamSynchronize(h->s->stream), "synchronize");
+    unsigned f = 0;
+    hgpu::cudaCheck(cudaMemcpy(&f, h->s->health, sizeof f, cudaMemcpyDeviceToHost), "health read");
+    if (f & (hgpu::HEALTH_NONFINITE_DT | hgpu::HEALTH_STATE_NONFINITE))
+        return fail(HGPU_ERR_NONFINITE, "health " + std::to_string(f) + ": a non-finite value in the state or the CFL reduction");
+    if (f & (hgpu::HEALTH_STATE_DENSITY | hgpu::HEALTH_STATE_PRESSURE))
+        return fail(HGPU_ERR_UNPHYSICAL, "health " + std::to_string(f) + ": density or pressure <= 0 in the state");
+    return HGPU_OK;
+}
 
 void destroyGraph(hgpu_solver* h) {
     if (h->exec) cudaGraphExecDestroy(h->exec);
@@ -112,6 +127,7 @@ const char* hgpu_status_string(int status) {
     case HGPU_ERR_ARG: return "HGPU_ERR_ARG";
     case HGPU_ERR_UNSUPPORTED: return "HGPU_ERR_UNSUPPORTED";
     case HGPU_ERR_NOMEM: return "HGPU_ERR_NOMEM";
+    case HGPU_ERR_UNPHYSICAL: return "HGPU_ERR_UNPHYSICAL";
     }
     return "HGPU_ERR_UNKNOWN";
 }
@@ -186,7 +202,7 @@ int hgpu_set_state_potential(hgpu_solver* h, const void* host_state, size_t coun
         const bool wasLive = h->s->potentialLive();
         h->s->resetState(host_state, count, host_potential);
         if (h->s->potentialLive() != wasLive) destroyGraph(h);   // the step's kernels differ
-        return (int)HGPU_OK;
+        return healthStatus(h);
     });
 }
 
@@ -205,7 +221,7 @@ int hgpu_update(hgpu_solver* h, int nsteps, double* last_dt) {
     return guarded([&]() {
         runSteps(h, nsteps);
         if (last_dt) *last_dt = h->s->lastDt();
-        return (int)HGPU_OK;
+        return healthStatus(h);
     });
 }
 
@@ -233,7 +249,7 @@ int hgpu_update_host(hgpu_solver* h, const void* host_in, size_t in_count, int n
         }
         const double dt = h->s->lastDt();   // waits for the stream, which waited for the copies
         if (last_dt) *last_dt = dt;
-        return (int)HGPU_OK;
+        return healthStatus(h);
     });
 }
 
@@ -261,6 +277,18 @@ int hgpu_health(hgpu_solver* h, uint32_t* flags) {
         hgpu::cudaCheck(cudaMemcpy(&f, h->s->health, sizeof f, cudaMemcpyDeviceToHost), "health read");
         hgpu::cudaCheck(cudaMemset(h->s->health, 0, sizeof f), "health clear");
         *flags = f;
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_set_health_mode(hgpu_solver* h, int mode) {
+    if (!h) return fail(HGPU_ERR_ARG, "null handle");
+    if (mode < HGPU_HEALTH_OFF || mode > HGPU_HEALTH_STRICT) return fail(HGPU_ERR_ARG, "unknown health mode");
+    return guarded([&]() {
+        const int checks = mode == HGPU_HEALTH_OFF ? 0 : 1;
+        if (checks != h->s->stateChecks) destroyGraph(h);   // the step's kernels differ
+        h->s->stateChecks = checks;
+        h->healthMode = mode;
         return (int)HGPU_OK;
     });
 }
@@ -524,6 +552,14 @@ int hgpu_batch_dts(hgpu_batch* b, double* dts, int n) {
 int hgpu_batch_health(hgpu_batch* b, uint32_t* flags) {
     if (!b || !flags) return fail(HGPU_ERR_ARG, "null argument");
     return guarded([&]() { *flags = b->b->readHealth(); return (int)HGPU_OK; });
+}
+
+int hgpu_batch_problem_health(hgpu_batch* b, uint32_t* flags, int n) {
+    if (!b || !flags) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        b->b->readProblemHealth(reinterpret_cast<unsigned*>(flags), n);
+        return (int)HGPU_OK;
+    });
 }
 
 int hgpu_batch_get_tuning(const hgpu_batch* b, hgpu_batch_tuning* t) {

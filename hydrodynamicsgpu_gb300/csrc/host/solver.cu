@@ -422,6 +422,7 @@ void Solver<real>::resetState(const void* host, size_t count, const void* pot) {
     // 100 x gaussSeidelMaxIter relaxations; they read the density, which the energy
     // update above does not touch
     if (rc.cfg.use_gravity) relaxPotential(state.as<real>(), 100 * rc.cfg.gauss_seidel_max_iter);
+    checkState();
     cudaCheck(cudaGetLastError(), "reset kernels");
     cudaCheck(cudaStreamSynchronize(stream), "set_state sync");
 }
@@ -605,6 +606,7 @@ void Solver<real>::hostStep(const void* in, void* out, bool upload, bool downloa
         };
     }
     step();
+    checkState();
     if (download && !banded) {
         cudaEvent_t stepped = pipeEvent(ev++);
         cudaCheck(cudaEventRecord(stepped, stream), "event record");
@@ -637,6 +639,15 @@ void Solver<real>::update() {                                // Solver::update (
         finalizeDt(false);
     }
     step();
+    checkState();
+}
+
+template <typename real>
+void Solver<real>::checkState() {
+    if (!this->stateChecks) return;
+    launch("state_check", 1, [&] {
+        launchStateCheck<real>(rc.grid, state.as<real>(), livePotential(), health, stream);
+    });
 }
 
 template <typename real>

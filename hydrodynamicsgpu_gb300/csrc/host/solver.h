@@ -205,6 +205,8 @@ public:
     virtual int numStates() const = 0;
     cudaStream_t stream = nullptr;
     unsigned* health = nullptr;       // device word
+    // state check after every step and upload (health.cuh): 0 off, 1 on (default)
+    int stateChecks = 1;
 };
 
 template <typename real>
@@ -220,6 +222,7 @@ public:
     const Equation& getEquation() const override { return *equation; }
     void update() override;                 // Solver::update (Solver.cpp:521-546)
     void boundary();                        // Solver::boundary (Solver.cpp:448-464)
+    void checkState();                      // the state check into the health word (health.cuh)
     void boundaryOn(real* buf);
     double lastDt() override;
     void* stateDevicePtr() override { return state.get(); }

@@ -14,6 +14,7 @@
 #include "reduce.cuh"
 #include "roe_cells.cuh"
 #include "batch_common.cuh"
+#include "health.cuh"
 
 namespace hgpu {
 namespace {
@@ -165,6 +166,26 @@ __global__ void __launch_bounds__(256) batchGravityKernel(const BatchProblem<rea
     }
 }
 
+// the state check (health.cuh) of every problem: bits into the problem's word and the batch's
+template <typename real, int D>
+__global__ void __launch_bounds__(256) batchStateCheckKernel(const BatchProblem<real>* __restrict__ P,
+                                                             const BatchTile* __restrict__ tiles, int nT,
+                                                             BatchTuning tu, const real* __restrict__ state,
+                                                             unsigned* health, unsigned* healthP, unsigned* q) {
+    for (;;) {
+        int t = nextItem(q);
+        if (t >= nT) break;
+        const BatchTile tl = tiles[t];
+        const BatchProblem<real>& pr = P[tl.p];
+        int x, y, z;
+        long long c;
+        unsigned bits = 0;
+        if (tileCell(pr.g, tl, tu, x, y, z, c))
+            bits = stateCheckCell<real, D>(pr.g, state + (long long)(D + 2) * pr.stateOff, nullptr, c, x, y, z);
+        warpHealthOr(bits, healthP + tl.p, health);
+    }
+}
+
 template <typename real, int D, bool HLL>
 __global__ void __launch_bounds__(256) batchWaveKernel(const BatchProblem<real>* __restrict__ P,
                                                        const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
@@ -263,6 +284,15 @@ void BatchLaunch<real>::combine(const real* fluxBuf, const CombinePlan<real>& pl
 template <typename real>
 void BatchLaunch<real>::gravity(int integ, const StepConst<real>* sc, unsigned* q) const {
 #define L(DD) batchGravityKernel<real, DD><<<persistentBlocks(batchGravityKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, integ, sc, state, q)
+    if (dim == 1) L(1);
+    else if (dim == 2) L(2);
+    else L(3);
+#undef L
+}
+
+template <typename real>
+void BatchLaunch<real>::stateCheck(unsigned* health, unsigned* healthP, unsigned* q) const {
+#define L(DD) batchStateCheckKernel<real, DD><<<persistentBlocks(batchStateCheckKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, state, health, healthP, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);

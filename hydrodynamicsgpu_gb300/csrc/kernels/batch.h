@@ -53,6 +53,8 @@ struct BatchLaunch {
               unsigned* health, unsigned* q) const;
     void combine(const real* fluxBuf, const CombinePlan<real>& plan, const StepConst<real>* sc, unsigned* q) const;
     void gravity(int integ, const StepConst<real>* sc, unsigned* q) const;
+    // the state check (health.cuh) of every problem: bits into healthP[p] and *health
+    void stateCheck(unsigned* health, unsigned* healthP, unsigned* q) const;
 };
 
 }  // namespace hgpu

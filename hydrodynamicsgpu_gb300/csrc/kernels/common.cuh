@@ -87,7 +87,15 @@ __host__ __device__ inline double bitsToDouble(unsigned long long b, bool isFloa
 }
 
 // ---- health word bits (hgpu_health) ----
-enum : unsigned int { HEALTH_NONFINITE_DT = 1u, HEALTH_HLLC_NOBRANCH = 2u };
+// (HGPU_HEALTH_* in include/hgpu/hgpu.h)
+enum : unsigned int {
+    HEALTH_NONFINITE_DT = 1u,       // a NaN in the CFL reduction
+    HEALTH_HLLC_NOBRANCH = 2u,      // an HLLC interface where no flux branch was taken
+    HEALTH_STATE_NONFINITE = 4u,    // a checked state holds a NaN or an infinity
+    HEALTH_STATE_DENSITY = 8u,      // a checked state has density <= 0
+    HEALTH_STATE_PRESSURE = 16u,    // a checked state has pressure <= 0
+    HEALTH_STATE_BITS = 28u
+};
 
 // ---- slope limiters: res/SlopeLimiter.cl:5-68, min/max with C-library fmin/fmax semantics ----
 // Literal types follow the reference source: `2.` is a double literal, so in the FP32

@@ -34,6 +34,7 @@ __device__ __forceinline__ bool isZeroBits(double x) {
     return ((__double2hiint(x) & 0x7FFFFFFF) | __double2loint(x)) == 0;
 }
 __device__ __forceinline__ bool geZero(float x) { return x >= 0.f; }
+__device__ __forceinline__ bool isZeroBits(float x) { return (__float_as_int(x) & 0x7FFFFFFF) == 0; }
 
 // .5 * x exactly: decrement the exponent of a normal x whose half is normal.  The
 // rare other operands (zero, subnormal, Inf, NaN) take the FP64 unit out of line, so

@@ -94,6 +94,11 @@ template <typename real>
 void launchDisplay(const Grid& g, real gamma, int method, const real* state, float* out, cudaStream_t st,
                    const real* pot = nullptr);
 
+// ---- health.cu: the state check (health.cuh) of every interior cell into *health;
+// pot: the potential, or null for a zero potential ----
+template <typename real>
+void launchStateCheck(const Grid& g, const real* state, const real* pot, unsigned* health, cudaStream_t st);
+
 // ---- tableaus (combine.cu): alpha/beta in double, order ----
 int tableauOrder(int integrator);
 double tableauAlpha(int integrator, int m, int k);

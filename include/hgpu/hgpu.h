@@ -43,7 +43,8 @@ typedef enum hgpu_status {
     HGPU_ERR_OOB = 5,         /* a size/offset argument is out of range       */
     HGPU_ERR_ARG = 6,         /* NULL handle/pointer or wrong element count   */
     HGPU_ERR_UNSUPPORTED = 7, /* combination not provided by this build       */
-    HGPU_ERR_NOMEM = 8        /* device allocation failed                     */
+    HGPU_ERR_NOMEM = 8,       /* device allocation failed                     */
+    HGPU_ERR_UNPHYSICAL = 9   /* density or pressure <= 0 in the state (strict health mode) */
 } hgpu_status;
 
 /* ---- solver family (src/HydroGPUApp.cpp:90-118 solver registry) ---- */
@@ -240,9 +241,28 @@ int hgpu_last_dt(hgpu_solver* s, double* dt);
  * CFL reduction (health word), HGPU_ERR_CUDA on a CUDA error. */
 int hgpu_synchronize(hgpu_solver* s);
 
-/* Read and clear the device-side health word (bit 0: non-finite dt seen;
- * bit 1: HLLC interface with no flux branch taken). */
+/* ---- failure detection.  The reference has none (it only throws at set-up:
+ *      src/Solver/Solver.cpp:150-153, 201); here every step ends, and every upload
+ *      is followed, by a check of the state's interior cells on the device. ---- */
+#define HGPU_HEALTH_NONFINITE_DT    1u   /* a NaN in the CFL reduction                            */
+#define HGPU_HEALTH_HLLC_NOBRANCH   2u   /* an HLLC interface where no flux branch was taken       */
+#define HGPU_HEALTH_STATE_NONFINITE 4u   /* a NaN or infinity in a checked state                   */
+#define HGPU_HEALTH_STATE_DENSITY   8u   /* density <= 0 in a checked state                        */
+#define HGPU_HEALTH_STATE_PRESSURE 16u   /* pressure <= 0: 2 rho (E - rho phi) <= |m|^2, rounded   */
+
+/* Read and clear the device-side health word (HGPU_HEALTH_* bits, ORed since the
+ * last read). */
 int hgpu_health(hgpu_solver* s, uint32_t* flags);
+
+/* What the state check does: HGPU_HEALTH_OFF skips it; HGPU_HEALTH_RECORD (the
+ * default) sets the health bits; HGPU_HEALTH_STRICT also makes hgpu_set_state,
+ * hgpu_set_state_potential, hgpu_update and hgpu_update_host wait for the stream and
+ * return HGPU_ERR_NONFINITE (non-finite state or dt) or HGPU_ERR_UNPHYSICAL
+ * (density or pressure <= 0) while such bits are set; the state is still written
+ * and the bits stay set until hgpu_health reads them.  The check reads the state
+ * once per step (one kernel). */
+enum { HGPU_HEALTH_OFF = 0, HGPU_HEALTH_RECORD = 1, HGPU_HEALTH_STRICT = 2 };
+int hgpu_set_health_mode(hgpu_solver* s, int mode);
 
 /* Device pointer of the current state buffer (for device-resident pipelines;
  * the buffer is owned by the solver). */
@@ -325,6 +345,10 @@ int hgpu_batch_timed_update(hgpu_batch* b, int nsteps, float* ms);
 /* dt of the most recent step of every problem (n = number of problems). */
 int hgpu_batch_dts(hgpu_batch* b, double* dts, int n);
 int hgpu_batch_health(hgpu_batch* b, uint32_t* flags);
+/* Read and clear every problem's own health word (HGPU_HEALTH_STATE_* bits of the
+ * state check that ends each batched step; n = number of problems).  No reference
+ * counterpart (the reference has no run-time checks, src/Solver/Solver.cpp:150-153). */
+int hgpu_batch_problem_health(hgpu_batch* b, uint32_t* flags, int n);
 int hgpu_batch_get_tuning(const hgpu_batch* b, hgpu_batch_tuning* t);
 int hgpu_batch_set_tuning(hgpu_batch* b, const hgpu_batch_tuning* t);
 /* Time candidate tunings for `steps` steps each on this batch (its state is restored
@@ -367,14 +391,17 @@ int hgpu_checkpoint_destroy(hgpu_checkpoint* c);
  * (hosts that own the whole device-memory budget through their own pool, code that
  * runs where allocation is forbidden, plug-in hosts that only lend their buffers).
  * Returns in *dt_out what Solver::calcTimestep would return for d_state (AoS, ghosts
- * included, the precision of cfg), i.e. cfl * min over interior cells and axes of the
- * cell timestep, and blocks until it is on the host.  Scratch is one fixed array
- * inside the library (about 512 KiB on every GPU that loads it, kept until exit), so
- * grids above 16,777,216 cells are rejected with HGPU_ERR_OOB.  The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the array: calls that overlap on
- * the GPU (different streams or threads at once) race and must be serialised by the
- * caller.  `stream` is a cudaStream_t or NULL. */
+ * included, the precision of cfg) with a zero gravitational potential, i.e. cfl * min
+ * over interior cells and axes of the cell timestep, and blocks until it is on the
+ * host; for a state a solver steps with a nonzero static potential it is not that
+ * solver's dt.  Scratch is one fixed array inside the library (about 512 KiB, kept
+ * until exit), so grids above 16,777,216 cells are rejected with HGPU_ERR_OOB.  The
+ * library's module is loaded lazily: the first call on a device loads it, which
+ * reserves the array on that device, and looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call at set-up, before the host's device
+ * memory is handed to a pool and before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (different streams or threads at once) race
+ * and must be serialised by the caller.  `stream` is a cudaStream_t or NULL. */
 int hgpu_cfl_timestep_noalloc(const hgpu_config* cfg, const void* d_state, double* dt_out, void* stream);
 
 /* Diagnostic: measured FP64 fused multiply-add issue rate of the current device

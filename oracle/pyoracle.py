@@ -36,10 +36,10 @@ def build_oracle(force=False):
     return LIB_ORACLE
 
 
-def build_refcl(quiet=True):
+def build_refcl(quiet=True, ref=None):
     sys.path.insert(0, os.path.join(HERE, "refcl"))
     import build_refcl  # noqa
-    return build_refcl.build(quiet=quiet)
+    return build_refcl.build(ref=ref, quiet=quiet)
 
 
 _lib = None

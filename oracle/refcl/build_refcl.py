@@ -179,8 +179,10 @@ def compile_variant(v, cxx="g++"):
 
 
 def build(ref=None, variants=None, jobs=None, quiet=True):
-    ref = ref or os.environ.get("HGPU_REFERENCE_DIR", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "res")):
+    """ref: the reference checkout (--ref, or the HGPU_REFERENCE_DIR environment
+    variable); without one, an existing _ref/gen/ is compiled as is."""
+    ref = ref or os.environ.get("HGPU_REFERENCE_DIR")
+    if ref and os.path.isdir(os.path.join(ref, "res")):
         generate(ref)
     elif not os.path.isdir(GEN):
         if not quiet:
@@ -197,7 +199,7 @@ def build(ref=None, variants=None, jobs=None, quiet=True):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=None)
+    ap.add_argument("--ref", default=None, help="the reference checkout (default: $HGPU_REFERENCE_DIR)")
     ap.add_argument("--jobs", type=int, default=None)
     args = ap.parse_args()
     build(args.ref, jobs=args.jobs, quiet=False)
