@@ -248,9 +248,11 @@ def batched_sweep(hg, _abi, ic, args):
     for p, x in enumerate(inits):
         b.set_state(p, x)
     b.update(3)
+    b.problem_health()
     batch_ms = b.timed_update(steps) / steps
     _, total_cells, kps = b.info()
     health = b.health()
+    flagged = b.problem_health()
     b.close()
     solvers = [hg.Solver(c) for c in cfgs]
     for s_, x in zip(solvers, inits):
@@ -279,7 +281,11 @@ def batched_sweep(hg, _abi, ic, args):
         "interior_cells": interior, "steps": steps,
         "batched": {"value": rate(batch_ms), "ms_per_step": batch_ms, "kernels_per_step": kps,
                     "tuning": {"tile": list(tuning[:3]), "staged_eigenbasis": tuning[3],
-                               "blocks_per_sm": tuning[4]}, "autotune_s": tune_s, "health_flags": health},
+                               "blocks_per_sm": tuning[4], "split_flux": tuning[5], "cells_per_thread": tuning[6]},
+                    "autotune_s": tune_s, "health_flags": health,
+                    "problems_flagged": {"count": int((flagged != 0).sum()),
+                                         "first": [int(i) for i in np.flatnonzero(flagged)[:8]],
+                                         "bits": int(np.bitwise_or.reduce(flagged)) if len(flagged) else 0}},
         "plain_sequential": {"value": rate(seq_ms), "ms_per_step": seq_ms},
         "plain_interleaved": {"value": rate(inter_ms), "ms_per_step": inter_ms},
         "speedup_vs_plain_sequential": seq_ms / batch_ms,

@@ -43,6 +43,7 @@ SIGNATURES = {
     "hgpu_synchronize": (ctypes.c_int, [_P]),
     "hgpu_health": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
     "hgpu_set_health_mode": (ctypes.c_int, [_P, ctypes.c_int]),
+    "hgpu_set_fused_stages": (ctypes.c_int, [_P, ctypes.c_int]),
     "hgpu_state_device_ptr": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "hgpu_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "hgpu_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
@@ -294,6 +295,10 @@ class Solver:
         check(lib().hgpu_health(self.h, ctypes.byref(f)))
         return f.value
 
+    def set_fused_stages(self, on):
+        """Each Runge-Kutta stage as two fused per-direction kernels (2D FP64 EulerRoe)."""
+        check(lib().hgpu_set_fused_stages(self.h, 1 if on else 0))
+
     def set_graphs(self, on):
         check(lib().hgpu_set_graphs(self.h, 1 if on else 0))
 
@@ -359,7 +364,8 @@ class Solver:
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int), ("tile_z", ctypes.c_int),
-                ("staged", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+                ("staged", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("split_flux", ctypes.c_int),
+                ("cells_per_thread", ctypes.c_int)]
 
 
 class Batch:
@@ -431,10 +437,13 @@ class Batch:
     def tuning(self):
         t = BatchTuning()
         check(lib().hgpu_batch_get_tuning(self.h, ctypes.byref(t)))
-        return (t.tile_x, t.tile_y, t.tile_z, t.staged, t.blocks_per_sm)
+        return (t.tile_x, t.tile_y, t.tile_z, t.staged, t.blocks_per_sm, t.split_flux, t.cells_per_thread)
 
-    def set_tuning(self, tile=(32, 8, 1), staged=1, blocks_per_sm=0):
-        t = BatchTuning(tile[0], tile[1], tile[2], staged, blocks_per_sm)
+    def set_tuning(self, tile=(32, 8, 1), staged=1, blocks_per_sm=0, split_flux=None, cells_per_thread=1):
+        """split_flux None keeps the current choice (the two-pass flux for FP64 EulerRoe)."""
+        if split_flux is None:
+            split_flux = self.tuning()[5]
+        t = BatchTuning(tile[0], tile[1], tile[2], staged, blocks_per_sm, split_flux, cells_per_thread)
         check(lib().hgpu_batch_set_tuning(self.h, ctypes.byref(t)))
 
     def autotune(self, cache_path=None, steps=2):

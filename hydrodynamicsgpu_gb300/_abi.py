@@ -19,6 +19,7 @@ STATUS_NAMES = {
 # health word bits (hgpu_health) and modes (hgpu_set_health_mode)
 HEALTH_NONFINITE_DT, HEALTH_HLLC_NOBRANCH, HEALTH_STATE_NONFINITE, HEALTH_STATE_DENSITY, HEALTH_STATE_PRESSURE = \
     1, 2, 4, 8, 16
+HEALTH_COPY_TIMEOUT = 32
 HEALTH_OFF, HEALTH_RECORD, HEALTH_STRICT = 0, 1, 2
 
 SOLVERS = {"EulerRoe": 0, "EulerHLLC": 1, "EulerHLL": 2}

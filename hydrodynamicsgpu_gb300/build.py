@@ -32,6 +32,7 @@ SOURCES = {
     "kernels/display.cu": ["--fmad=false"],
     "kernels/gravity.cu": ["--fmad=false"],
     "kernels/health.cu": ["--fmad=false"],
+    "kernels/roe_fused.cu": ["--fmad=false"],
     "host/fits.cu": [],
     "host/adjoint.cu": [],
     "host/batch_solver.cu": [],
@@ -42,7 +43,8 @@ SOURCES = {
 HEADERS = ["kernels/fp64ops.cuh", "kernels/common.cuh", "kernels/roe_cells.cuh", "kernels/hllc_cells.cuh",
            "kernels/combine_cells.cuh", "kernels/batch.h", "kernels/batch_common.cuh", "host/batch_solver.h", "kernels/roe.cuh", "kernels/reduce.cuh", "kernels/kernels.h", "host/solver.h",
            "kernels/adjoint.h", "host/adjoint.h",
-           "kernels/limiter_dual.cuh", "host/fits.h", "kernels/gravity.h", "kernels/health.cuh"]
+           "kernels/limiter_dual.cuh", "host/fits.h", "kernels/gravity.h", "kernels/health.cuh",
+           "kernels/tma.cuh"]
 
 
 def nvcc():

@@ -100,9 +100,10 @@ BatchSolver<real>::BatchSolver(const std::vector<hgpu_config>& cfgs) {
         alphaBinary_ = tableauAlphaIsBinary(integ_);
     }
     BatchTuning def{};
-    if (dim_ == 1) def = {256, 1, 1, 1, 0};
-    else if (dim_ == 2) def = {32, 8, 1, 1, 0};
-    else def = {32, 4, 2, 1, 0};
+    const int split = splitAvailable() ? 1 : 0;
+    if (dim_ == 1) def = {256, 1, 1, 1, 0, split, 1};
+    else if (dim_ == 2) def = {32, 8, 1, 1, 0, split, 1};
+    else def = {32, 4, 2, 1, 0, split, 1};
     setTuning(def);
     cudaCheck(cudaDeviceSynchronize(), "batch init");
 }
@@ -124,9 +125,19 @@ void BatchSolver<real>::dropGraph() {
 }
 
 template <typename real>
+bool BatchSolver<real>::splitAvailable() const {
+    return sizeof(real) == 8 && kind_ == HGPU_SOLVER_ROE;
+}
+
+template <typename real>
 void BatchSolver<real>::setTuning(const BatchTuning& tu) {
-    if (tu.tx < 1 || tu.ty < 1 || tu.tz < 1 || tu.tx * tu.ty * tu.tz > 256)
-        throw ConfigError(HGPU_ERR_CONFIG, "tile must have between 1 and 256 cells");
+    if (tu.cpt < 1 || tu.cpt > 8) throw ConfigError(HGPU_ERR_CONFIG, "cells per thread must be 1 to 8");
+    if (tu.blocksPerSM < -1) throw ConfigError(HGPU_ERR_CONFIG, "blocks per SM must be >= -1");
+    if (tu.tx < 1 || tu.ty < 1 || tu.tz < 1 || tu.tx * tu.ty * tu.tz > 256 * tu.cpt)
+        throw ConfigError(HGPU_ERR_CONFIG, "tile must have between 1 and 256 x (cells per thread) cells");
+    if (tu.staged && tu.tx * tu.ty * tu.tz > 256)
+        throw ConfigError(HGPU_ERR_CONFIG, "a staged eigenbasis tile has at most 256 cells");
+    if (tu.split && !splitAvailable()) throw ConfigError(HGPU_ERR_UNSUPPORTED, "the two-pass flux is FP64 EulerRoe only");
     tuning_ = tu;
     std::vector<BatchTile> tiles;
     for (size_t p = 0; p < host_.size(); ++p) {
@@ -180,8 +191,14 @@ void BatchSolver<real>::update() {                       // Solver::update for e
             L.deltaQ(2, 1, in, dq_.as<real>(), nextQ());
             ++launches_;
         }
-        L.flux(kind_ == HGPU_SOLVER_ROE ? 0 : (kind_ == HGPU_SOLVER_HLL ? 2 : 1), lim, sc, in,
-               hllc_ ? nullptr : dq_.as<real>(), flux_.as<real>(), health, nextQ());
+        if (tuning_.split) {
+            unsigned* q0 = nextQ();
+            L.fluxSplit(lim, sc, in, dq_.as<real>(), flux_.as<real>(), q0, nextQ());
+            ++launches_;
+        } else {
+            L.flux(kind_ == HGPU_SOLVER_ROE ? 0 : (kind_ == HGPU_SOLVER_HLL ? 2 : 1), lim, sc, in,
+                   hllc_ ? nullptr : dq_.as<real>(), flux_.as<real>(), health, nextQ());
+        }
         L.combine(flux_.as<real>(), plan, sc, nextQ());
         launches_ += 2;
     };
@@ -306,7 +323,7 @@ std::string BatchSolver<real>::signature() const {
             h *= 1099511628211ULL;
         }
     std::ostringstream s;
-    s << (kind_ == HGPU_SOLVER_ROE ? "roe" : kind_ == HGPU_SOLVER_HLL ? "hll" : "hllc") << "-" << dim_ << "d-i" << integ_ << "-" << (sizeof(real) == 8 ? "f64" : "f32")
+    s << "v2-" << (kind_ == HGPU_SOLVER_ROE ? "roe" : kind_ == HGPU_SOLVER_HLL ? "hll" : "hllc") << "-" << dim_ << "d-i" << integ_ << "-" << (sizeof(real) == 8 ? "f64" : "f32")
       << "-p" << host_.size() << "-" << std::hex << h;
     return s.str();
 }
@@ -321,7 +338,8 @@ bool BatchSolver<real>::loadTuning(const std::string& path) {
         std::string key;
         BatchTuning tu{};
         double ms = 0;
-        if (ls >> key >> tu.tx >> tu.ty >> tu.tz >> tu.staged >> tu.blocksPerSM >> ms && key == sig) {
+        if (ls >> key >> tu.tx >> tu.ty >> tu.tz >> tu.staged >> tu.blocksPerSM >> tu.split >> tu.cpt >> ms &&
+            key == sig) {
             setTuning(tu);
             tunedMs_ = ms;
             return true;
@@ -337,6 +355,16 @@ void BatchSolver<real>::autotune(const std::string& cachePath, int steps) {
     size_t bytes = sizeof(real) * (size_t)totalCells_ * N_;
     DeviceBuffer saved(bytes, false);
     cudaCheck(cudaMemcpyAsync(saved.get(), state_.get(), bytes, cudaMemcpyDeviceToDevice, stream), "save state");
+    auto timeOf = [&](const BatchTuning& c) {
+        setTuning(c);
+        cudaCheck(cudaMemcpyAsync(state_.get(), saved.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
+        run(1);                                              // capture + warm
+        float ms = timedRun(steps);
+        return ms / std::max(1, steps);
+    };
+    // 1) tile shape x eigenbasis staging x blocks per SM, one cell per thread, with the
+    //    two-pass flux where it exists
+    const int split = splitAvailable() ? 1 : 0;
     std::vector<BatchTuning> cands;
     std::vector<std::array<int, 3>> shapes;
     if (dim_ == 1) shapes = {{256, 1, 1}, {128, 1, 1}};
@@ -344,18 +372,36 @@ void BatchSolver<real>::autotune(const std::string& cachePath, int steps) {
     else shapes = {{32, 4, 2}, {16, 4, 4}, {8, 8, 4}, {32, 2, 2}};
     for (auto& s : shapes)
         for (int staged = 0; staged < 2; ++staged)
-            for (int bps : {0, 2}) {
+            for (int bps : {0, 2, -1}) {
                 if (hllc_ && staged == 0) continue;           // staging only changes the Roe eigenbasis
-                cands.push_back({s[0], s[1], s[2], hllc_ ? 1 : staged, bps});
+                cands.push_back({s[0], s[1], s[2], hllc_ ? 1 : staged, bps, split, 1});
             }
     BatchTuning best = tuning_;
     double bestMs = 1e30;
     for (const auto& c : cands) {
-        setTuning(c);
-        cudaCheck(cudaMemcpyAsync(state_.get(), saved.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
-        run(1);                                              // capture + warm
-        float ms = timedRun(steps);
-        double per = ms / std::max(1, steps);
+        double per = timeOf(c);
+        if (per < bestMs) { bestMs = per; best = c; }
+    }
+    // 2) threads per cell: 1, 1/2 or 1/4 (each thread takes 1, 2 or 4 cells of a tile
+    //    that many times larger along its slowest axis; unstaged eigenbasis), and the
+    //    one-pass flux against the two-pass one
+    std::vector<BatchTuning> second;
+    for (int cpt : {1, 2, 4})
+        for (int sp = 0; sp <= split; ++sp) {
+            BatchTuning c = best;
+            c.cpt = cpt;
+            c.split = sp;
+            if (cpt > 1) {
+                c.staged = 0;
+                if (dim_ == 1) c.tx *= cpt;
+                else if (dim_ == 2) c.ty *= cpt;
+                else c.tz *= cpt;
+            }
+            if (c.cpt == best.cpt && c.split == best.split) continue;
+            second.push_back(c);
+        }
+    for (const auto& c : second) {
+        double per = timeOf(c);
         if (per < bestMs) { bestMs = per; best = c; }
     }
     setTuning(best);
@@ -365,7 +411,7 @@ void BatchSolver<real>::autotune(const std::string& cachePath, int steps) {
     if (!cachePath.empty()) {
         std::ofstream f(cachePath, std::ios::app);
         f << signature() << " " << best.tx << " " << best.ty << " " << best.tz << " " << best.staged << " "
-          << best.blocksPerSM << " " << bestMs << "\n";
+          << best.blocksPerSM << " " << best.split << " " << best.cpt << " " << bestMs << "\n";
     }
 }
 

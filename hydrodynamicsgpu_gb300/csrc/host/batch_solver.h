@@ -67,6 +67,7 @@ private:
     void ensureGraph();
     void dropGraph();
     void checkProblem(int p, size_t count) const;
+    bool splitAvailable() const;             // the two-pass flux exists (FP64 EulerRoe)
     std::string signature() const;
     bool loadTuning(const std::string& path);
 };

@@ -67,6 +67,8 @@ int healthStatus(hgpu_solver* h) {
     hgpu::cudaCheck(cudaStreamSynchronize(h->s->stream), "synchronize");
     unsigned f = 0;
     hgpu::cudaCheck(cudaMemcpy(&f, h->s->health, sizeof f, cudaMemcpyDeviceToHost), "health read");
+    if (f & hgpu::HEALTH_COPY_TIMEOUT)
+        return fail(HGPU_ERR_TIMEOUT, "health " + std::to_string(f) + ": a bounded wait for a bulk copy gave up");
     if (f & (hgpu::HEALTH_NONFINITE_DT | hgpu::HEALTH_STATE_NONFINITE))
         return fail(HGPU_ERR_NONFINITE, "health " + std::to_string(f) + ": a non-finite value in the state or the CFL reduction");
     if (f & (hgpu::HEALTH_STATE_DENSITY | hgpu::HEALTH_STATE_PRESSURE))
@@ -264,6 +266,7 @@ int hgpu_synchronize(hgpu_solver* h) {
         hgpu::cudaCheck(cudaStreamSynchronize(h->s->stream), "synchronize");
         unsigned flags = 0;
         hgpu::cudaCheck(cudaMemcpy(&flags, h->s->health, sizeof flags, cudaMemcpyDeviceToHost), "health read");
+        if (flags & hgpu::HEALTH_COPY_TIMEOUT) return fail(HGPU_ERR_TIMEOUT, "a bounded wait for a bulk copy gave up");
         if (flags & hgpu::HEALTH_NONFINITE_DT) return fail(HGPU_ERR_NONFINITE, "non-finite value in the CFL reduction");
         return (int)HGPU_OK;
     });
@@ -289,6 +292,16 @@ int hgpu_set_health_mode(hgpu_solver* h, int mode) {
         if (checks != h->s->stateChecks) destroyGraph(h);   // the step's kernels differ
         h->s->stateChecks = checks;
         h->healthMode = mode;
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_set_fused_stages(hgpu_solver* h, int enabled) {
+    if (!h) return fail(HGPU_ERR_ARG, "null handle");
+    return guarded([&]() {
+        const int st = h->s->setFusedStages(enabled != 0);
+        if (st != HGPU_OK) return fail(st, "fused stages: 2D FP64 EulerRoe with a Runge-Kutta integrator only");
+        destroyGraph(h);                                     // the step's kernels differ
         return (int)HGPU_OK;
     });
 }
@@ -565,14 +578,15 @@ int hgpu_batch_problem_health(hgpu_batch* b, uint32_t* flags, int n) {
 int hgpu_batch_get_tuning(const hgpu_batch* b, hgpu_batch_tuning* t) {
     if (!b || !t) return fail(HGPU_ERR_ARG, "null argument");
     hgpu::BatchTuning tu = b->b->tuning();
-    *t = {tu.tx, tu.ty, tu.tz, tu.staged, tu.blocksPerSM};
+    *t = {tu.tx, tu.ty, tu.tz, tu.staged, tu.blocksPerSM, tu.split, tu.cpt};
     return HGPU_OK;
 }
 
 int hgpu_batch_set_tuning(hgpu_batch* b, const hgpu_batch_tuning* t) {
     if (!b || !t) return fail(HGPU_ERR_ARG, "null argument");
     return guarded([&]() {
-        b->b->setTuning({t->tile_x, t->tile_y, t->tile_z, t->staged, t->blocks_per_sm});
+        b->b->setTuning({t->tile_x, t->tile_y, t->tile_z, t->staged, t->blocks_per_sm, t->split_flux,
+                         t->cells_per_thread});
         return (int)HGPU_OK;
     });
 }

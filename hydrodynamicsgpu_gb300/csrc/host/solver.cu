@@ -1,6 +1,8 @@
 // solver.cu -- host side of the GB300 Euler update: configuration, buffers, the
 // step sequence and the Runge-Kutta stage plans.  Host code only (built by nvcc
 // so the launchers' CUDA types resolve); the kernels live in ../kernels/.
+#include <type_traits>
+
 #include "solver.h"
 
 #include <algorithm>
@@ -167,6 +169,13 @@ void ForwardEuler<real>::integrate(const std::function<void(real* stage)>& compu
     });
 }
 
+// ForwardEuler updates its stage buffer (the state) in place, which a kernel that also
+// reads its neighbours' stage values cannot do; solvers keep it on the unfused path.
+template <typename real>
+void ForwardEuler<real>::integrateFused(const std::function<void(real*, const CombinePlan<real>&)>&) {
+    throw ConfigError(HGPU_ERR_UNSUPPORTED, "fused stages need a Runge-Kutta integrator");
+}
+
 template <typename real>
 void ForwardEuler<real>::integrateZeroDeriv() {
     Solver<real>* s = this->solver;
@@ -303,6 +312,12 @@ void RungeKutta<real>::integrate(const std::function<void(real* stage)>& compute
             launchDerivCombine<real>(s->rc.grid, s->ph, s->flux.template as<real>(), plans_[k], s->sc(), s->stream);
         });
     }
+}
+
+// the same stages; plans_[k] never writes the slot stage k reads (buildStagePlans)
+template <typename real>
+void RungeKutta<real>::integrateFused(const std::function<void(real*, const CombinePlan<real>&)>& stageKernel) {
+    for (int k = 0; k < order_; ++k) stageKernel(plans_[k].slot[inputSlot_[k]], plans_[k]);
 }
 
 template <typename real>
@@ -583,7 +598,7 @@ void Solver<real>::hostStep(const void* in, void* out, bool upload, bool downloa
     }
     finalizeDt(false);
 
-    const bool banded = download && integrator->lastCombineWritesState();
+    const bool banded = download && integrator->lastCombineWritesState() && !fusedActive();
     struct Unhook {
         Integrator<real>* i;
         ~Unhook() { i->lastCombine = nullptr; }
@@ -720,7 +735,56 @@ void Roe<real>::calcFlux(real* stage) {                      // Roe::calcDeriv (
 
 template <typename real>
 void Roe<real>::step() {                                     // Roe::step (Roe.cpp:94-99)
+    if (fused_) {
+        this->integrator->integrateFused([this](real* stage, const CombinePlan<real>& plan) { fusedStage(stage, plan); });
+        return;
+    }
     this->integrator->integrate([this](real* stage) { calcFlux(stage); });
+}
+
+// The fused form of Roe::calcDeriv + the integrator's combine for one stage (2D FP64;
+// kernels/roe_fused.cu): x pass, then y pass with the divergence and the combine.  The
+// flux buffer holds the x part of the divergence between them.
+template <typename real>
+void Roe<real>::fusedStage(real* stage, const CombinePlan<real>& plan) {
+    if constexpr (std::is_same<real, double>::value) {
+        const bool seam = this->rc.cfg.compat == HGPU_COMPAT_SEAM;
+        if (seam && stage != this->state.template as<real>()) this->boundaryOn(stage);
+        const void* tm = tensorMapFor(stage);
+        this->launch("roe_stage_fused", 2, [&] {
+            launchRoeStageFused(this->rc.grid, this->ph, this->rc.cfg.limiter, this->sc(), stage,
+                                basis.template as<double>(), this->flux.template as<double>(), plan, seam, tm,
+                                this->health, this->stream);
+        });
+    } else {
+        (void)stage;
+        (void)plan;
+        throw ConfigError(HGPU_ERR_UNSUPPORTED, "fused stages are FP64 only");
+    }
+}
+
+template <typename real>
+const void* Roe<real>::tensorMapFor(const real* stage) {
+    auto it = tensorMaps_.find(stage);
+    if (it != tensorMaps_.end()) return it->second.bytes;
+    TensorMap m{};
+    std::string err;
+    if (roeFusedTensorMapSize() > sizeof m.bytes ||
+        !makeRoeFusedTensorMap(this->rc.grid, reinterpret_cast<const double*>(stage), m.bytes, err))
+        throw ConfigError(HGPU_ERR_CUDA, "fused stage tensor map: " + err);
+    return tensorMaps_.emplace(stage, m).first->second.bytes;
+}
+
+template <typename real>
+int Roe<real>::setFusedStages(bool on) {
+    if (!on) {
+        fused_ = false;
+        return HGPU_OK;
+    }
+    if (sizeof(real) != 8 || this->rc.dim != 2 || this->integrator->order() < 2) return HGPU_ERR_UNSUPPORTED;
+    roeFusedPrepare();
+    fused_ = true;
+    return HGPU_OK;
 }
 
 template <typename real>

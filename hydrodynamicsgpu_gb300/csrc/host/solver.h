@@ -11,6 +11,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <functional>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -104,6 +105,9 @@ public:
     virtual ~Integrator() = default;
     // computeFlux(stage) must leave the interface fluxes of `stage` in the solver's flux buffer
     virtual void integrate(const std::function<void(real* stage)>& computeFlux) = 0;
+    // the same stages, each done by stageKernel(stage, plan): a kernel that forms the
+    // stage's flux divergence itself and applies the combine `plan` of this stage
+    virtual void integrateFused(const std::function<void(real* stage, const CombinePlan<real>& plan)>& stageKernel) = 0;
     // the self-gravity pass with a zero potential (SelfGravitation::applyPotential)
     virtual void integrateZeroDeriv() = 0;
     // the self-gravity pass with a live potential: per callback the relaxation sweeps
@@ -125,6 +129,7 @@ class ForwardEuler : public Integrator<real> {        // src/Integrator/ForwardE
 public:
     using Integrator<real>::Integrator;
     void integrate(const std::function<void(real* stage)>& computeFlux) override;
+    void integrateFused(const std::function<void(real* stage, const CombinePlan<real>& plan)>& stageKernel) override;
     void integrateZeroDeriv() override;
     void integrateGravity() override;
     int order() const override { return 1; }
@@ -136,6 +141,7 @@ class RungeKutta : public Integrator<real> {          // include/HydroGPU/Integr
 public:
     RungeKutta(Solver<real>* s, int tableau);
     void integrate(const std::function<void(real* stage)>& computeFlux) override;
+    void integrateFused(const std::function<void(real* stage, const CombinePlan<real>& plan)>& stageKernel) override;
     void integrateZeroDeriv() override;
     void integrateGravity() override;
     int order() const override { return order_; }
@@ -201,6 +207,8 @@ public:
     virtual bool hostPipelined() const = 0;
     virtual void hostStep(const void* in, void* out, bool upload, bool download) = 0;
     virtual size_t volume() const = 0;
+    // run each Runge-Kutta stage as fused kernels (2D FP64 EulerRoe; HGPU_ERR_UNSUPPORTED otherwise)
+    virtual int setFusedStages(bool on) { return on ? HGPU_ERR_UNSUPPORTED : HGPU_OK; }
     virtual int dim() const = 0;
     virtual int numStates() const = 0;
     cudaStream_t stream = nullptr;
@@ -268,6 +276,8 @@ protected:
     virtual int slowTile() const { return 1; }
     virtual void bandedPrologueWork(int tile0, int tiles) { (void)tile0; (void)tiles; }
     virtual void bandedPrologueEnd() {}
+    // the stages run as fused kernels (no separate combine to cut in bands)
+    virtual bool fusedActive() const { return false; }
 
 private:
     cudaStream_t copyStream_ = nullptr;     // update_host's uploads and downloads
@@ -289,6 +299,12 @@ public:
     using FiniteVolumeSolver<real>::FiniteVolumeSolver;
 protected:
     DeviceBuffer basis, deltaQTilde;
+    bool fused_ = false;
+    struct alignas(64) TensorMap { unsigned char bytes[128]; };
+    std::map<const void*, TensorMap> tensorMaps_;     // per stage buffer, for the fused y pass
+    const void* tensorMapFor(const real* stage);
+    void fusedStage(real* stage, const CombinePlan<real>& plan);
+    bool fusedActive() const override { return fused_; }
     void initBuffers() override;
     void initFlux();                              // calcEigenBasis once per step
     void cflReduce();                             // calcCellTimestep + the min-reduction
@@ -299,6 +315,8 @@ protected:
     int slowTile() const override { return roeBasisSlowTile(this->rc.dim); }
     void bandedPrologueWork(int tile0, int tiles) override;
     void bandedPrologueEnd() override { cflReduce(); }
+public:
+    int setFusedStages(bool on) override;
 };
 
 template <typename real>

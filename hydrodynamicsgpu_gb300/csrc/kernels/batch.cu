@@ -45,9 +45,7 @@ __global__ void __launch_bounds__(256) batchRoeBasisKernel(const BatchProblem<re
                                                            real* __restrict__ basis, unsigned* q) {
     extern __shared__ unsigned char smem[];
     RoePrim<real, D>* prim = reinterpret_cast<RoePrim<real, D>*>(smem);
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
         const real* s = state + (long long)(D + 2) * pr.stateOff;
@@ -55,9 +53,10 @@ __global__ void __launch_bounds__(256) batchRoeBasisKernel(const BatchProblem<re
         if (tu.staged) {
             roeBasisTile<real, D>(pr.g, pr.ph, s, b, loA, hiA, tl.x0, tl.y0, tl.z0, tu.tx, tu.ty, tu.tz, prim);
         } else {
+            for (int r = 0; r < tu.cpt; ++r) {
             int x, y, z;
             long long c;
-            if (tileCell(pr.g, tl, tu, x, y, z, c)) {
+            if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) {
                 const int NB = RoeRec<D>::NB;
                 real sR[D + 2], sL[D + 2], rec[NB];
                 loadState<real, D>(s, c, sR);
@@ -72,6 +71,7 @@ __global__ void __launch_bounds__(256) batchRoeBasisKernel(const BatchProblem<re
                     for (int k = 0; k < NB; ++k) b[((long long)side * NB + k) * pr.g.V + c] = rec[k];
                 }
             }
+            }
         }
     }
 }
@@ -81,18 +81,19 @@ __global__ void __launch_bounds__(256) batchDtKernel(const BatchProblem<real>* _
                                                      const BatchTile* __restrict__ tiles, int nT, BatchTuning tu, int hllc,
                                                      const real* __restrict__ faces, unsigned long long* acc,
                                                      unsigned* health, unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
         int x, y, z;
         long long c;
         unsigned long long best = ~0ULL;
         bool nan = false;
-        if (tileCell(pr.g, tl, tu, x, y, z, c))
-            best = hllc ? hllcDtCell<real, D>(pr.g, pr.ph, faces + pr.faceOff, c, x, y, z, nan)
-                        : roeDtCell<real, D>(pr.g, pr.ph, faces + pr.faceOff, c, x, y, z, nan);
+        for (int r = 0; r < tu.cpt; ++r)
+            if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) {
+                unsigned long long b = hllc ? hllcDtCell<real, D>(pr.g, pr.ph, faces + pr.faceOff, c, x, y, z, nan)
+                                            : roeDtCell<real, D>(pr.g, pr.ph, faces + pr.faceOff, c, x, y, z, nan);
+                best = b < best ? b : best;
+            }
         if (nan) atomicOr(health, HEALTH_NONFINITE_DT);
         blockMinToGlobal(best, acc + tl.p);
     }
@@ -113,14 +114,13 @@ __global__ void __launch_bounds__(256) batchDeltaQKernel(const BatchProblem<real
                                                          int loA, int hiA, const real* __restrict__ stage,
                                                          const real* __restrict__ basis, real* __restrict__ dq,
                                                          unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
         int x, y, z;
         long long c;
-        if (tileCell(pr.g, tl, tu, x, y, z, c))
+        for (int r = 0; r < tu.cpt; ++r)
+        if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
             roeDeltaQCell<real, D>(pr.g, stage + (long long)(D + 2) * pr.stateOff, basis + pr.faceOff, dq + pr.dqOff, c,
                                    x, y, z, loA, hiA);
     }
@@ -131,14 +131,13 @@ __global__ void __launch_bounds__(256) batchCombineKernel(const BatchProblem<rea
                                                           const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                           const real* __restrict__ flux, CombinePlan<real> plan,
                                                           const StepConst<real>* __restrict__ sc, unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
         int x, y, z;
         long long c;
-        if (tileCell(pr.g, tl, tu, x, y, z, c))
+        for (int r = 0; r < tu.cpt; ++r)
+        if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
             derivCombineCell<real, D, D>(pr.g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
     }
 }
@@ -150,19 +149,20 @@ __global__ void __launch_bounds__(256) batchGravityKernel(const BatchProblem<rea
                                                           const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                           int integ, const StepConst<real>* __restrict__ sc,
                                                           real* __restrict__ state, unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
-        int x, y, z;
-        long long c;
-        if (!tileCell(pr.g, tl, tu, x, y, z, c)) continue;
-        real* s = state + (long long)(D + 2) * (pr.stateOff + c);
-        const StepConst<real>& k = sc[tl.p];
+        for (int r = 0; r < tu.cpt; ++r) {
+            int x, y, z;
+            long long c;
+            if (!tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
+            real* s = state + (long long)(D + 2) * (pr.stateOff + c);
+            const StepConst<real>& k = sc[tl.p];
 #pragma unroll
-        for (int j = 0; j < D + 2; ++j)
-            s[j] = integ == HGPU_INTEGRATOR_FORWARD_EULER ? s[j] + (real)0. * k.dt : alphaOnlyElem<real>(integ, s[j], k);
+            for (int j = 0; j < D + 2; ++j)
+                s[j] = integ == HGPU_INTEGRATOR_FORWARD_EULER ? s[j] + (real)0. * k.dt
+                                                               : alphaOnlyElem<real>(integ, s[j], k);
+        }
     }
 }
 
@@ -172,16 +172,15 @@ __global__ void __launch_bounds__(256) batchStateCheckKernel(const BatchProblem<
                                                              const BatchTile* __restrict__ tiles, int nT,
                                                              BatchTuning tu, const real* __restrict__ state,
                                                              unsigned* health, unsigned* healthP, unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
         int x, y, z;
         long long c;
         unsigned bits = 0;
-        if (tileCell(pr.g, tl, tu, x, y, z, c))
-            bits = stateCheckCell<real, D>(pr.g, state + (long long)(D + 2) * pr.stateOff, nullptr, c, x, y, z);
+        for (int r = 0; r < tu.cpt; ++r)
+        if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
+            bits |= stateCheckCell<real, D>(pr.g, state + (long long)(D + 2) * pr.stateOff, nullptr, c, x, y, z);
         warpHealthOr(bits, healthP + tl.p, health);
     }
 }
@@ -191,17 +190,17 @@ __global__ void __launch_bounds__(256) batchWaveKernel(const BatchProblem<real>*
                                                        const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                        const real* __restrict__ state, real* __restrict__ waves,
                                                        unsigned* q) {
-    for (;;) {
-        int t = nextItem(q);
-        if (t >= nT) break;
+    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
-        int x, y, z;
-        long long c;
-        if (!tileCell(pr.g, tl, tu, x, y, z, c)) continue;
         double gq = ((double)pr.ph.gamma + 1.) / (2. * (double)pr.ph.gamma);
-        hllcWaveCell<real, D, HLL>(pr.g, pr.ph, gq, state + (long long)(D + 2) * pr.stateOff, waves + pr.faceOff, c, x,
-                                   y, z);
+        for (int r = 0; r < tu.cpt; ++r) {
+            int x, y, z;
+            long long c;
+            if (!tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
+            hllcWaveCell<real, D, HLL>(pr.g, pr.ph, gq, state + (long long)(D + 2) * pr.stateOff, waves + pr.faceOff, c,
+                                       x, y, z);
+        }
     }
 }
 
@@ -209,9 +208,9 @@ __global__ void __launch_bounds__(256) batchWaveKernel(const BatchProblem<real>*
 
 template <typename real>
 void BatchLaunch<real>::boundary(unsigned* q) const {
-    if (dim == 1) batchBoundaryKernel<real, 1><<<persistentBlocks(batchBoundaryKernel<real, 1>, 0, tu.blocksPerSM), 256, 0, st>>>(P, nP, state, q);
-    else if (dim == 2) batchBoundaryKernel<real, 2><<<persistentBlocks(batchBoundaryKernel<real, 2>, 0, tu.blocksPerSM), 256, 0, st>>>(P, nP, state, q);
-    else batchBoundaryKernel<real, 3><<<persistentBlocks(batchBoundaryKernel<real, 3>, 0, tu.blocksPerSM), 256, 0, st>>>(P, nP, state, q);
+    if (dim == 1) batchBoundaryKernel<real, 1><<<persistentBlocks(batchBoundaryKernel<real, 1>, 0, tu.blocksPerSM, nP), 256, 0, st>>>(P, nP, state, q);
+    else if (dim == 2) batchBoundaryKernel<real, 2><<<persistentBlocks(batchBoundaryKernel<real, 2>, 0, tu.blocksPerSM, nP), 256, 0, st>>>(P, nP, state, q);
+    else batchBoundaryKernel<real, 3><<<persistentBlocks(batchBoundaryKernel<real, 3>, 0, tu.blocksPerSM, nP), 256, 0, st>>>(P, nP, state, q);
 }
 
 template <typename real>
@@ -225,7 +224,7 @@ template <typename real>
 void BatchLaunch<real>::roeBasis(int loA, int hiA, unsigned* q) const {
     int smem = tu.staged ? primSmem<real>(dim, tu) : 0;
 #define L(DD)                                                                                                      \
-    batchRoeBasisKernel<real, DD><<<persistentBlocks(batchRoeBasisKernel<real, DD>, smem, tu.blocksPerSM), 256, smem, \
+    batchRoeBasisKernel<real, DD><<<persistentBlocks(batchRoeBasisKernel<real, DD>, smem, tu.blocksPerSM, nT), 256, smem, \
                                     st>>>(P, tiles, nT, tu, loA, hiA, state, faces, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
@@ -235,7 +234,7 @@ void BatchLaunch<real>::roeBasis(int loA, int hiA, unsigned* q) const {
 
 template <typename real>
 void BatchLaunch<real>::waves(int hll, unsigned* q) const {
-#define L(DD, H) batchWaveKernel<real, DD, H><<<persistentBlocks(batchWaveKernel<real, DD, H>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, state, faces, q)
+#define L(DD, H) batchWaveKernel<real, DD, H><<<persistentBlocks(batchWaveKernel<real, DD, H>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, state, faces, q)
     if (hll) {
         if (dim == 1) L(1, true);
         else if (dim == 2) L(2, true);
@@ -250,7 +249,7 @@ void BatchLaunch<real>::waves(int hll, unsigned* q) const {
 
 template <typename real>
 void BatchLaunch<real>::dt(int hllc, unsigned long long* acc, unsigned* health, unsigned* q) const {
-#define L(DD) batchDtKernel<real, DD><<<persistentBlocks(batchDtKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, hllc, faces, acc, health, q)
+#define L(DD) batchDtKernel<real, DD><<<persistentBlocks(batchDtKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, hllc, faces, acc, health, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);
@@ -264,7 +263,7 @@ void BatchLaunch<real>::finalize(int integ, unsigned long long* acc, StepConst<r
 
 template <typename real>
 void BatchLaunch<real>::deltaQ(int loA, int hiA, const real* stage, real* dq, unsigned* q) const {
-#define L(DD) batchDeltaQKernel<real, DD><<<persistentBlocks(batchDeltaQKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, loA, hiA, stage, faces, dq, q)
+#define L(DD) batchDeltaQKernel<real, DD><<<persistentBlocks(batchDeltaQKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, loA, hiA, stage, faces, dq, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);
@@ -274,7 +273,7 @@ void BatchLaunch<real>::deltaQ(int loA, int hiA, const real* stage, real* dq, un
 template <typename real>
 void BatchLaunch<real>::combine(const real* fluxBuf, const CombinePlan<real>& plan, const StepConst<real>* sc,
                                 unsigned* q) const {
-#define L(DD) batchCombineKernel<real, DD><<<persistentBlocks(batchCombineKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, fluxBuf, plan, sc, q)
+#define L(DD) batchCombineKernel<real, DD><<<persistentBlocks(batchCombineKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, fluxBuf, plan, sc, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);
@@ -283,7 +282,7 @@ void BatchLaunch<real>::combine(const real* fluxBuf, const CombinePlan<real>& pl
 
 template <typename real>
 void BatchLaunch<real>::gravity(int integ, const StepConst<real>* sc, unsigned* q) const {
-#define L(DD) batchGravityKernel<real, DD><<<persistentBlocks(batchGravityKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, integ, sc, state, q)
+#define L(DD) batchGravityKernel<real, DD><<<persistentBlocks(batchGravityKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, integ, sc, state, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);
@@ -292,7 +291,7 @@ void BatchLaunch<real>::gravity(int integ, const StepConst<real>* sc, unsigned* 
 
 template <typename real>
 void BatchLaunch<real>::stateCheck(unsigned* health, unsigned* healthP, unsigned* q) const {
-#define L(DD) batchStateCheckKernel<real, DD><<<persistentBlocks(batchStateCheckKernel<real, DD>, 0, tu.blocksPerSM), 256, 0, st>>>(P, tiles, nT, tu, state, health, healthP, q)
+#define L(DD) batchStateCheckKernel<real, DD><<<persistentBlocks(batchStateCheckKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, state, health, healthP, q)
     if (dim == 1) L(1);
     else if (dim == 2) L(2);
     else L(3);

@@ -26,9 +26,11 @@ struct BatchTile {
 
 // Launch shape chosen by the autotuner.
 struct BatchTuning {
-    int tx, ty, tz;      // tile shape (tx*ty*tz <= 256 threads)
+    int tx, ty, tz;      // tile shape (tx*ty*tz <= 256 * cpt cells)
     int staged;          // eigenbasis: per-cell primitives staged in shared memory (1) or recomputed per face (0)
     int blocksPerSM;     // persistent blocks per SM (0 = as many as fit)
+    int split;           // FP64 EulerRoe flux in two passes (corrections, then transforms) instead of one
+    int cpt;             // cells per thread: each of a block's 256 threads takes cpt cells of the tile
 };
 
 template <typename real>
@@ -51,6 +53,9 @@ struct BatchLaunch {
     // kind: 0 EulerRoe, 1 EulerHLLC, 2 EulerHLL
     void flux(int kind, int lim, const StepConst<real>* sc, const real* stage, const real* dq, real* fluxBuf,
               unsigned* health, unsigned* q) const;
+    // the FP64 EulerRoe flux as two passes (q0: corrections, q1: transforms); real = double only
+    void fluxSplit(int lim, const StepConst<real>* sc, const real* stage, const real* dq, real* fluxBuf, unsigned* q0,
+                   unsigned* q1) const;
     void combine(const real* fluxBuf, const CombinePlan<real>& plan, const StepConst<real>* sc, unsigned* q) const;
     void gravity(int integ, const StepConst<real>* sc, unsigned* q) const;
     // the state check (health.cuh) of every problem: bits into healthP[p] and *health

@@ -15,10 +15,11 @@ __device__ __forceinline__ int nextItem(unsigned* q) {
     return item;
 }
 
-// the cell of this thread inside a tile, or false if outside the tile/grid
-__device__ __forceinline__ bool tileCell(const Grid& g, const BatchTile& t, const BatchTuning& tu, int& x, int& y, int& z,
-                                         long long& c) {
-    int tx = threadIdx.x % tu.tx, ty = (threadIdx.x / tu.tx) % tu.ty, tz = threadIdx.x / (tu.tx * tu.ty);
+// cell `i` of a tile (i = threadIdx.x + r * blockDim.x for the thread's r-th cell,
+// r < tu.cpt), or false if outside the tile/grid
+__device__ __forceinline__ bool tileCell(const Grid& g, const BatchTile& t, const BatchTuning& tu, int i, int& x,
+                                         int& y, int& z, long long& c) {
+    int tx = i % tu.tx, ty = (i / tu.tx) % tu.ty, tz = i / (tu.tx * tu.ty);
     x = t.x0 + tx;
     y = t.y0 + ty;
     z = t.z0 + tz;
@@ -26,9 +27,24 @@ __device__ __forceinline__ bool tileCell(const Grid& g, const BatchTile& t, cons
     c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
     return true;
 }
+__device__ __forceinline__ bool tileCell(const Grid& g, const BatchTile& t, const BatchTuning& tu, int& x, int& y, int& z,
+                                         long long& c) {
+    return tileCell(g, t, tu, (int)threadIdx.x, x, y, z, c);
+}
+
+// The tile kernels run either persistent (perSM >= 0: SMs x blocks per SM blocks pull
+// tiles from the queue) or one block per work item (perSM < 0: `items` blocks, block b
+// takes item b, no queue).
+__device__ __forceinline__ int firstItem(unsigned* q, const BatchTuning& tu) {
+    return tu.blocksPerSM < 0 ? (int)blockIdx.x : nextItem(q);
+}
+__device__ __forceinline__ int nextItemAfter(unsigned* q, const BatchTuning& tu) {
+    return tu.blocksPerSM < 0 ? 0x7fffffff : nextItem(q);
+}
 
 template <typename K>
-int persistentBlocks(K kernel, int smem, int perSM) {
+int persistentBlocks(K kernel, int smem, int perSM, int items) {
+    if (perSM < 0) return items;
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -94,6 +94,7 @@ enum : unsigned int {
     HEALTH_STATE_NONFINITE = 4u,    // a checked state holds a NaN or an infinity
     HEALTH_STATE_DENSITY = 8u,      // a checked state has density <= 0
     HEALTH_STATE_PRESSURE = 16u,    // a checked state has pressure <= 0
+    HEALTH_COPY_TIMEOUT = 32u,      // a bounded wait for a bulk copy (TMA) gave up
     HEALTH_STATE_BITS = 28u
 };
 

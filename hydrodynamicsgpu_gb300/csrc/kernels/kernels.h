@@ -1,6 +1,7 @@
 // kernels.h -- host-side launchers of the sm_103a Euler kernels (plain C++ types).
 #pragma once
 #include <cuda_runtime.h>
+#include <string>
 #include "common.cuh"
 
 namespace hgpu {
@@ -98,6 +99,18 @@ void launchDisplay(const Grid& g, real gamma, int method, const real* state, flo
 // pot: the potential, or null for a zero potential ----
 template <typename real>
 void launchStateCheck(const Grid& g, const real* state, const real* pot, unsigned* health, cudaStream_t st);
+
+// ---- roe_fused.cu: the 2D FP64 EulerRoe stage as two fused per-direction kernels
+// (x pass, then y pass with the divergence and the integrator's combine), FP64 2D only.
+// tensorMap: from makeRoeFusedTensorMap for `stage` (roeFusedTensorMapSize() bytes,
+// 64-byte aligned); dX: V x 4 doubles of scratch for the x part of the divergence.
+// The plan must not write the stage buffer (Runge-Kutta stages; not ForwardEuler). ----
+size_t roeFusedTensorMapSize();
+bool makeRoeFusedTensorMap(const Grid& g, const double* stage, void* out, std::string& err);
+void roeFusedPrepare();
+void launchRoeStageFused(const Grid& g, const Phys<double>& ph, int limiter, const StepConst<double>* sc,
+                         const double* stage, const double* basis, double* dX, const CombinePlan<double>& plan,
+                         int seam, const void* tensorMap, unsigned* health, cudaStream_t st);
 
 // ---- tableaus (combine.cu): alpha/beta in double, order ----
 int tableauOrder(int integrator);

@@ -249,6 +249,7 @@ int hgpu_synchronize(hgpu_solver* s);
 #define HGPU_HEALTH_STATE_NONFINITE 4u   /* a NaN or infinity in a checked state                   */
 #define HGPU_HEALTH_STATE_DENSITY   8u   /* density <= 0 in a checked state                        */
 #define HGPU_HEALTH_STATE_PRESSURE 16u   /* pressure <= 0: 2 rho (E - rho phi) <= |m|^2, rounded   */
+#define HGPU_HEALTH_COPY_TIMEOUT   32u   /* a bounded wait for a bulk copy gave up (work skipped)  */
 
 /* Read and clear the device-side health word (HGPU_HEALTH_* bits, ORed since the
  * last read). */
@@ -274,6 +275,17 @@ int hgpu_stream(hgpu_solver* s, void** stream);
 /* Use CUDA-graph replay for hgpu_update (default on; off runs the same kernels
  * as plain launches). */
 int hgpu_set_graphs(hgpu_solver* s, int enabled);
+
+/* Run each Runge-Kutta stage as two fused per-direction kernels instead of four
+ * (EulerRoe, FP64, 2D, a Runge-Kutta integrator; HGPU_ERR_UNSUPPORTED otherwise):
+ * the reference's calcDeltaQTilde, calcFlux, calcFluxDeriv and multAdd of a stage
+ * (src/Solver/Roe.cpp:101-112, res/Roe.cl:152-320, res/CalcFluxDeriv.cl:7-44,
+ * res/Common.cl:201-210) become an x pass (stage rows staged by bulk copies; the
+ * Delta-q-tilde and limited flux of x faces in shared memory; the x part of each
+ * cell's divergence) and a y pass (stage rows staged by 2D tensor copies while it
+ * marches down 32-column strips; y faces, divergence and the integrator's combine).
+ * Same operations, same bits as the default four kernels.  Off by default. */
+int hgpu_set_fused_stages(hgpu_solver* s, int enabled);
 
 /* Number of kernels one step launches (for launch accounting). */
 int hgpu_kernels_per_step(const hgpu_solver* s, int* count);
@@ -325,9 +337,14 @@ int hgpu_save_fits(hgpu_solver* s, const char* directory, int* save_index);
 typedef struct hgpu_batch hgpu_batch;
 
 typedef struct hgpu_batch_tuning {
-    int tile_x, tile_y, tile_z;   /* cells per work tile (product <= 256)            */
-    int staged;                   /* Roe eigenbasis: per-cell values via shared memory */
-    int blocks_per_sm;            /* persistent blocks per SM, 0 = occupancy limit     */
+    int tile_x, tile_y, tile_z;   /* cells per work tile (product <= 256 x cells_per_thread) */
+    int staged;                   /* Roe eigenbasis: per-cell values via shared memory
+                                     (tiles of at most 256 cells)                        */
+    int blocks_per_sm;            /* persistent blocks per SM pulling tiles from the queue,
+                                     0 = occupancy limit; -1 = one block per tile, no queue */
+    int split_flux;               /* FP64 EulerRoe: the flux in two passes (corrections,
+                                     then transforms) instead of one                     */
+    int cells_per_thread;         /* 1..8: threads per cell = 1 / cells_per_thread       */
 } hgpu_batch_tuning;
 
 int hgpu_batch_create(const hgpu_config* cfgs, int nproblems, hgpu_batch** out);

@@ -96,12 +96,17 @@ def test_roe_batch_limiters(hg, limiter):
 
 
 @pytest.mark.parametrize("dim,tunings", [
-    (1, [((256, 1, 1), 1, 0), ((128, 1, 1), 0, 2), ((7, 1, 1), 1, 1)]),
-    (2, [((32, 8, 1), 1, 0), ((16, 16, 1), 0, 0), ((64, 4, 1), 1, 2), ((5, 3, 1), 1, 1), ((16, 8, 1), 0, 1)]),
-    (3, [((32, 4, 2), 1, 0), ((8, 8, 4), 0, 2), ((3, 5, 2), 1, 1)]),
+    (1, [((256, 1, 1), 1, 0), ((128, 1, 1), 0, 2), ((7, 1, 1), 1, 1), ((512, 1, 1), 0, 0, 1, 2),
+         ((256, 1, 1), 1, 0, 0, 1), ((256, 1, 1), 0, -1, 1, 1)]),
+    (2, [((32, 8, 1), 1, 0), ((16, 16, 1), 0, 0), ((64, 4, 1), 1, 2), ((5, 3, 1), 1, 1), ((16, 8, 1), 0, 1),
+         ((32, 8, 1), 1, 0, 0, 1), ((32, 16, 1), 0, 0, 1, 2), ((32, 32, 1), 0, 2, 0, 4), ((7, 9, 1), 0, 0, 1, 3),
+         ((16, 16, 1), 1, -1, 1, 1), ((32, 16, 1), 0, -1, 0, 2)]),
+    (3, [((32, 4, 2), 1, 0), ((8, 8, 4), 0, 2), ((3, 5, 2), 1, 1), ((32, 4, 4), 0, 0, 1, 2),
+         ((32, 4, 2), 1, 0, 0, 1), ((32, 4, 2), 1, -1, 1, 1)]),
 ])
 def test_batch_tuning_invariant(hg, dim, tunings):
-    """Every tile shape, staging choice and persistent grid gives the same bits."""
+    """Every tile shape, staging choice, persistent grid, flux form (one or two passes)
+    and number of cells per thread gives the same bits."""
     check_batch(hg, mixed_configs("EulerRoe", dim, "RungeKutta4", "MinMod", n=5, seed=20 + dim), steps=2,
                 tunings=tunings)
 
@@ -174,7 +179,7 @@ def test_batch_autotune_cache(hg, tmp_path):
     finally:
         b.close()
     lines = open(cache).read().split("\n")
-    assert lines[0].startswith("roe-2d-")
+    assert lines[0].startswith("v2-roe-2d-")
     b2 = hg.Batch(cfgs)
     try:
         assert b2.autotune(cache, steps=1) == tu          # looked up, not re-timed
@@ -198,7 +203,8 @@ def test_batch_info_and_health(hg):
         n, cells, k = b.info()
         assert n == 5
         assert cells >= sum(c.size[0] * c.size[1] for c in cfgs)
-        assert k == 1 + 2 + 1 + 2 * 3            # boundary, basis, dt, finalize, RK2: 2 x (dq, flux, combine)
+        # boundary, basis, dt, finalize; RK2: 2 x (dq, flux corrections, flux transforms, combine); state check
+        assert k == 1 + 2 + 1 + 2 * 4 + 1
         assert b.health() == 0
         with pytest.raises(hg.HgpuError):
             b.set_state(5, inits[0])
