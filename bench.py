@@ -528,7 +528,7 @@ MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 568.0, "roe_delta_q_tilde": 252.0, "roe
 # instructions x 32) over the cells of a KH 512x512 step of the same kernels; roe_flux
 # is its two passes together (corrections 30.6 + transforms 65.5).
 FP64_PIPE_PER_CELL = {"roe_eigenbasis": 71.4, "cfl_min_reduce": 9.9, "roe_delta_q_tilde": 37.7,
-                      "roe_flux": 96.1, "flux_divergence_combine": 40.9, "state_check": 7.0}
+                      "roe_flux": 96.1, "flux_divergence_combine": 40.9, "state_check": 2.0}
 
 
 def fp64_roofline(prof, value, fp64_peak):

@@ -16,7 +16,8 @@ from ._abi import (COMPAT_REF, COMPAT_SEAM, FP32, FP64, HgpuConfig, INTEGRATORS,
                    SOLVERS, make_config)
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libhgpu.so")
+# HGPU_LIBRARY selects another build of the library (the checked one: libhgpu_checked.so)
+LIB_PATH = os.environ.get("HGPU_LIBRARY") or os.path.join(PKG, "libhgpu.so")
 
 # every entry point of include/hgpu/hgpu.h: name -> (restype, argtypes)
 _P = ctypes.c_void_p
@@ -52,6 +53,7 @@ SIGNATURES = {
     "hgpu_timed_update": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "hgpu_profile_update": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "hgpu_fp64_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "hgpu_checked_status": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32)]),
     "hgpu_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "hgpu_host_free": (ctypes.c_int, [_P]),
     "hgpu_cfl_timestep_noalloc": (ctypes.c_int, [_CFG, _P, ctypes.POINTER(ctypes.c_double), _P]),

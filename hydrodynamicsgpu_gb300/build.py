@@ -14,6 +14,10 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhgpu.so")
+# the checked variant (HGPU_CHECKED: index tests in the kernels, guard bands around
+# every device allocation), built on request for the checked test suite
+BUILD_CHECKED = os.path.join(PKG, "_build_checked")
+LIB_CHECKED = os.path.join(PKG, "libhgpu_checked.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -61,8 +65,8 @@ def _stale(obj, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, extra, verbose):
-    obj = os.path.join(BUILD, src.replace("/", "_").replace(".cu", ".o"))
+def _compile(src, extra, verbose, build_dir=BUILD):
+    obj = os.path.join(build_dir, src.replace("/", "_").replace(".cu", ".o"))
     deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] + \
            [os.path.join(REPO, "include", "hgpu", "hgpu.h"), os.path.abspath(__file__)]
     if not _stale(obj, deps):
@@ -77,19 +81,21 @@ def _compile(src, extra, verbose):
     return obj
 
 
-def build(verbose=False, jobs=None):
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, jobs=None, checked=False):
+    build_dir, lib = (BUILD_CHECKED, LIB_CHECKED) if checked else (BUILD, LIB)
+    flags = ["-DHGPU_CHECKED"] if checked else []
+    os.makedirs(build_dir, exist_ok=True)
     jobs = jobs or min(len(SOURCES), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(jobs) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), SOURCES.items()))
-    if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1] + flags, verbose, build_dir), SOURCES.items()))
+    if _stale(lib, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s" % r.stderr[-4000:])
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+        os.replace(lib + ".tmp", lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, checked="--checked" in sys.argv))

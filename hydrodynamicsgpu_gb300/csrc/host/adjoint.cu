@@ -11,6 +11,7 @@
 namespace hgpu {
 
 RoeAdjoint::RoeAdjoint(const ResolvedConfig& rc, cudaStream_t stream) : rc_(rc), stream_(stream) {
+    rc_.grid.check = checkWord();
     if (rc.cfg.solver != HGPU_SOLVER_ROE || rc.cfg.precision != HGPU_FP64 || rc.cfg.compat != HGPU_COMPAT_REF)
         throw ConfigError(HGPU_ERR_UNSUPPORTED, "the adjoint covers EulerRoe in FP64 with the REF scheme");
     for (int i = 0; i < 3; ++i) {

@@ -49,6 +49,7 @@ BatchSolver<real>::BatchSolver(const std::vector<hgpu_config>& cfgs) {
     for (const auto& r : rcs_) {
         BatchProblem<real> p{};
         p.g = r.grid;
+        p.g.check = checkWord();
         for (int i = 0; i < 3; ++i) {
             p.ph.dx[i] = (real)r.dx[i];
             p.ph.rdx[i] = (real)1 / p.ph.dx[i];

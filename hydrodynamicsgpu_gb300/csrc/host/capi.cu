@@ -296,6 +296,16 @@ int hgpu_set_health_mode(hgpu_solver* h, int mode) {
     });
 }
 
+int hgpu_checked_status(uint32_t* flags) {
+    if (!flags) return fail(HGPU_ERR_ARG, "null argument");
+    return guarded([&]() {
+        std::string where;
+        *flags = hgpu::takeChecks(where);
+        if (*flags) hgpu::setLastError(where);
+        return (int)HGPU_OK;
+    });
+}
+
 int hgpu_set_fused_stages(hgpu_solver* h, int enabled) {
     if (!h) return fail(HGPU_ERR_ARG, "null handle");
     return guarded([&]() {

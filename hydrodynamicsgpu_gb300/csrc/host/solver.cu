@@ -12,8 +12,69 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 
 namespace hgpu {
+
+#ifdef HGPU_CHECKED
+namespace {
+__device__ unsigned g_checkWord;               // CHECK_INDEX bits of the kernels' index tests
+constexpr size_t kGuard = 4096;                 // bytes of each guard band
+constexpr int kGuardByte = 0xA5;
+std::mutex g_guardMu;
+std::map<void*, size_t> g_guarded;              // user pointer -> bytes of every live buffer
+}  // namespace
+#endif
+
+unsigned* checkWord() {
+#ifdef HGPU_CHECKED
+    static std::mutex mu;
+    static unsigned* ptrs[64] = {};
+    int dev = 0;
+    cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64) return nullptr;
+    if (!ptrs[dev]) {
+        void* p = nullptr;
+        cudaCheck(cudaGetSymbolAddress(&p, g_checkWord), "check word address");
+        ptrs[dev] = static_cast<unsigned*>(p);
+    }
+    return ptrs[dev];
+#else
+    return nullptr;
+#endif
+}
+
+unsigned takeChecks(std::string& where) {
+#ifdef HGPU_CHECKED
+    cudaCheck(cudaDeviceSynchronize(), "synchronize");
+    unsigned f = 0, zero = 0;
+    cudaCheck(cudaMemcpyFromSymbol(&f, g_checkWord, sizeof f), "check word read");
+    cudaCheck(cudaMemcpyToSymbol(g_checkWord, &zero, sizeof zero), "check word clear");
+    if (f) where = "a kernel computed a cell index outside its grid";
+    std::vector<unsigned char> band(kGuard);
+    std::lock_guard<std::mutex> lock(g_guardMu);
+    for (const auto& kv : g_guarded) {
+        const unsigned char* p = static_cast<const unsigned char*>(kv.first);
+        for (const unsigned char* b : {p - kGuard, p + kv.second}) {
+            cudaCheck(cudaMemcpy(band.data(), b, kGuard, cudaMemcpyDeviceToHost), "guard band read");
+            for (unsigned char v : band)
+                if (v != (unsigned char)kGuardByte) {
+                    if (!(f & CHECK_GUARD))
+                        where = "a write landed in the guard band " + std::string(b < p ? "before" : "after") +
+                                " a buffer of " + std::to_string(kv.second) + " bytes";
+                    f |= CHECK_GUARD;
+                    break;
+                }
+        }
+    }
+    return f;
+#else
+    (void)where;
+    throw ConfigError(HGPU_ERR_UNSUPPORTED, "this library was built without HGPU_CHECKED");
+#endif
+}
 
 void cudaCheck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw CudaError(e, std::string(what) + ": " + cudaGetErrorString(e));
@@ -21,7 +82,20 @@ void cudaCheck(cudaError_t e, const char* what) {
 
 DeviceBuffer::DeviceBuffer(size_t bytes, bool zero) : bytes_(bytes) {
     if (bytes == 0) return;
+#ifdef HGPU_CHECKED
+    void* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, bytes + 2 * kGuard);
+    if (e == cudaSuccess) {
+        ptr_ = static_cast<unsigned char*>(base) + kGuard;
+        cudaCheck(cudaMemset(base, kGuardByte, kGuard), "guard band");
+        cudaCheck(cudaMemset(static_cast<unsigned char*>(ptr_) + bytes, kGuardByte, kGuard), "guard band");
+        cudaCheck(cudaStreamSynchronize(nullptr), "guard band sync");
+        std::lock_guard<std::mutex> lock(g_guardMu);
+        g_guarded[ptr_] = bytes;
+    }
+#else
     cudaError_t e = cudaMalloc(&ptr_, bytes);
+#endif
     if (e != cudaSuccess) {
         ptr_ = nullptr;
         (void)cudaGetLastError();
@@ -35,13 +109,25 @@ DeviceBuffer::DeviceBuffer(size_t bytes, bool zero) : bytes_(bytes) {
     }
 }
 
-DeviceBuffer::~DeviceBuffer() {
-    if (ptr_) cudaFree(ptr_);
+void DeviceBuffer::release() {
+    if (!ptr_) return;
+#ifdef HGPU_CHECKED
+    {
+        std::lock_guard<std::mutex> lock(g_guardMu);
+        g_guarded.erase(ptr_);
+    }
+    cudaFree(static_cast<unsigned char*>(ptr_) - kGuard);
+#else
+    cudaFree(ptr_);
+#endif
+    ptr_ = nullptr;
 }
+
+DeviceBuffer::~DeviceBuffer() { release(); }
 
 DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
     if (this != &o) {
-        if (ptr_) cudaFree(ptr_);
+        release();
         ptr_ = o.ptr_; bytes_ = o.bytes_;
         o.ptr_ = nullptr; o.bytes_ = 0;
     }
@@ -352,6 +438,7 @@ void RungeKutta<real>::integrateGravity() {
 // ---------------- Solver ----------------
 template <typename real>
 Solver<real>::Solver(const ResolvedConfig& rc_) : rc(rc_) {
+    rc.grid.check = checkWord();
     for (int i = 0; i < 3; ++i) {
         ph.dx[i] = (real)rc.dx[i];
         ph.rdx[i] = (real)1 / ph.dx[i];

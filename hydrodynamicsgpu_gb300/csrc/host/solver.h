@@ -50,7 +50,18 @@ public:
 private:
     void* ptr_ = nullptr;
     size_t bytes_ = 0;
+    void release();
 };
+
+// ---- checked build (HGPU_CHECKED) ----
+// Every DeviceBuffer then carries guard bands of a fixed byte pattern on both sides,
+// and kernel bodies test their cell indices (common.cuh cellOk) into one device word.
+// checkWord(): that word's device address for the current device (null in the normal
+// build).  takeChecks(): waits for the device, then returns and clears the word's
+// CHECK_INDEX bit and adds CHECK_GUARD if any live buffer's guard band changed
+// (`where` names the first); throws ConfigError(HGPU_ERR_UNSUPPORTED) in the normal build.
+unsigned* checkWord();
+unsigned takeChecks(std::string& where);
 
 // Validated configuration with the program-preamble constants resolved
 // (src/Solver/Solver.cpp:260-315, src/HydroGPUApp.cpp:164-226).

@@ -63,6 +63,7 @@ __device__ __forceinline__ void boundaryLine(const Grid& g, int axis, int N, int
     long long base = c[0] + (long long)g.S[0] * (c[1] + (long long)g.S[1] * c[2]);
     long long st = g.step[axis];
     int S = g.S[axis];
+    if (!cellOk(g, base) || !cellOk(g, base + (long long)(S - 1) * st)) return;
     for (int j = 0; j < N; ++j) {
         real* p = state + j;
 #define AT(k) p[(long long)N * (base + (long long)(k) * st)]
@@ -106,8 +107,12 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
                                                  long long c, int x, int y, int z, long long off) {
     const int N = D + 2;
     real d[N];
+    if (!cellOk(g, c)) return;
     // calcFluxDeriv: interior cells only, deriv[j] -= (F[i+1] - F[i]) / dx, sides ascending, from 0
     if (inRange(g, x, y, z, 2, 2)) {
+#pragma unroll
+        for (int side = 0; side < D; ++side)
+            if (!cellOk(g, c + g.step[side])) return;
 #pragma unroll
         for (int side = 0; side < D; ++side) {
 #pragma unroll

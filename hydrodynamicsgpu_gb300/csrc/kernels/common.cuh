@@ -22,7 +22,23 @@ struct Grid {
     int dim;
     long long step[3];   // cell stride per axis
     long long V;         // S[0]*S[1]*S[2]
+    unsigned* check = nullptr;   // checked builds: device word for index violations
 };
+
+// ---- checked build (compiled with HGPU_CHECKED): every cell index a kernel body
+// computes is tested against the grid before it is used; a violation ORs
+// CHECK_INDEX into *g.check and the access is skipped (no trap).  In the normal build
+// the test is the constant true and compiles away. ----
+enum : unsigned int { CHECK_INDEX = 1u, CHECK_GUARD = 2u };
+#ifdef HGPU_CHECKED
+__device__ __forceinline__ bool cellOk(const Grid& g, long long c) {
+    if (c >= 0 && c < g.V) return true;
+    if (g.check) atomicOr(g.check, CHECK_INDEX);
+    return false;
+}
+#else
+__device__ __forceinline__ constexpr bool cellOk(const Grid&, long long) { return true; }
+#endif
 
 __host__ __device__ inline void cellCoords(const Grid& g, long long c, int& x, int& y, int& z) {
     x = (int)(c % g.S[0]);

@@ -21,7 +21,7 @@ namespace hgpu {
 template <typename real, int D>
 __device__ __forceinline__ unsigned stateCheckCell(const Grid& g, const real* __restrict__ s,
                                                    const real* __restrict__ pot, long long c, int x, int y, int z) {
-    if (!inRange(g, x, y, z, 2, 2)) return 0u;
+    if (!inRange(g, x, y, z, 2, 2) || !cellOk(g, c)) return 0u;
     const int N = D + 2;
     real u[N];
 #pragma unroll

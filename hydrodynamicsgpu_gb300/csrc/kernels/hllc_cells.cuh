@@ -47,6 +47,7 @@ template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, double gq, const real* __restrict__ state,
                                          real* __restrict__ waves, long long c,
         const real* __restrict__ pot = nullptr) {
+    if (!cellOk(g, c) || !cellOk(g, c - g.step[SIDE])) return;
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
@@ -76,6 +77,7 @@ template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void hllWaveFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ state,
                                             real* __restrict__ waves, long long c,
         const real* __restrict__ pot = nullptr) {
+    if (!cellOk(g, c) || !cellOk(g, c - g.step[SIDE])) return;
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
@@ -130,6 +132,7 @@ __device__ __forceinline__ unsigned long long hllcDtCell(const Grid& g, const Ph
     if (inRange(g, x, y, z, 2, 1)) {
 #pragma unroll
         for (int side = 0; side < D; ++side) {
+            if (!cellOk(g, c) || !cellOk(g, c + g.step[side])) continue;
             real srHere = waves[((long long)side * 2 + 1) * g.V + c];
             real slNext = waves[((long long)side * 2 + 0) * g.V + c + g.step[side]];
             real minLambda = (real)fminLibm(0., (double)slNext);
@@ -148,6 +151,7 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
                                          const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c,
         const real* __restrict__ pot = nullptr) {
     const int N = D + 2, E = N - 1;
+    if (!cellOk(g, c) || !cellOk(g, c - g.step[SIDE])) return true;
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
     loadRotated<real, D, SIDE>(stage, c, stR);
@@ -217,6 +221,7 @@ __device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, con
                                         const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c,
         const real* __restrict__ pot = nullptr) {
     const int N = D + 2, E = N - 1;
+    if (!cellOk(g, c) || !cellOk(g, c - g.step[SIDE])) return true;
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
     loadRotated<real, D, SIDE>(stage, c, stR);

@@ -62,8 +62,9 @@ __device__ __forceinline__ void roeBasisTile(const Grid& g, const Phys<real>& ph
     __syncthreads();
     const int tx = threadIdx.x % TX, ty = (threadIdx.x / TX) % TY, tz = threadIdx.x / (TX * TY);
     const int x = x0 + tx, y = y0 + ty, z = z0 + tz;
-    if (tz < TZ && x < g.S[0] && y < g.S[1] && z < g.S[2]) {
-        const long long c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
+    const long long cc = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
+    if (tz < TZ && x < g.S[0] && y < g.S[1] && z < g.S[2] && cellOk(g, cc)) {
+        const long long c = cc;
         const int self = (tz + oz) * HY * HX + (ty + oy) * HX + (tx + ox);
         if (roeFace(g, 0, x, y, z, loA, hiA))
             storeFace<real, D, 0, GRAV>(g, prim[self - 1], prim[self], ph.gamma, basis, c);
@@ -87,6 +88,7 @@ __device__ __forceinline__ unsigned long long roeDtCell(const Grid& g, const Phy
     unsigned long long best = ~0ULL;
 #pragma unroll
     for (int side = 0; side < D; ++side) {
+        if (!cellOk(g, c) || !cellOk(g, c + g.step[side])) continue;
         real lamMax = basis[((long long)side * R_::NB + R_::LAME) * g.V + c];
         real lamMin = basis[((long long)side * R_::NB + R_::LAM0) * g.V + c + g.step[side]];
         real maxLambda = fmaxLibm((real)0., lamMax);
@@ -103,6 +105,7 @@ template <typename real, int D, int SIDE>
 __device__ __forceinline__ void deltaQFace(const Grid& g, const real* __restrict__ stage, const real* __restrict__ basis,
                                            real* __restrict__ dq, long long c, const real* sR) {
     const int N = D + 2, NB = RoeRec<D>::NB;
+    if (!cellOk(g, c - g.step[SIDE])) return;
     real sL[N], rec[NB], ds[N], y[N];
     loadState<real, D>(stage, c - g.step[SIDE], sL);
 #pragma unroll
@@ -119,6 +122,7 @@ template <typename real, int D>
 __device__ __forceinline__ void roeDeltaQCell(const Grid& g, const real* __restrict__ stage,
                                               const real* __restrict__ basis, real* __restrict__ dq, long long c,
                                               int x, int y, int z, int loA, int hiA) {
+    if (!cellOk(g, c)) return;
     real sR[D + 2];
     loadState<real, D>(stage, c, sR);
     if (roeFace(g, 0, x, y, z, loA, hiA)) deltaQFace<real, D, 0>(g, stage, basis, dq, c, sR);
@@ -134,6 +138,7 @@ __device__ __forceinline__ void fluxFace(const Grid& g, int lim, real dt_dx, con
     const int N = D + 2, NB = RoeRec<D>::NB;
     real sL[N], rec[NB], qL[N], q[N], qR[N], F[N];
     const long long st = g.step[SIDE];
+    if (!cellOk(g, c - st) || !cellOk(g, c + st)) return;
     loadState<real, D>(stage, c - st, sL);
 #pragma unroll
     for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)SIDE * NB + k) * g.V + c];
@@ -156,6 +161,7 @@ __device__ __forceinline__ void roeFluxCell(const Grid& g, int lim, const StepCo
                                             const real* __restrict__ stage, const real* __restrict__ basis,
                                             const real* __restrict__ dq, real* __restrict__ flux, long long c, int x,
                                             int y, int z, real* __restrict__ tape = nullptr) {
+    if (!cellOk(g, c)) return;
     real sR[D + 2];
     loadState<real, D>(stage, c, sR);
     if (roeFace(g, 0, x, y, z, 2, 1))
@@ -180,6 +186,7 @@ __device__ __forceinline__ void roeFluxCorrectionsCell(const Grid& g, int lim, c
     for (int side = 0; side < D; ++side) {
         if (!roeFace(g, side, x, y, z, 2, 1)) continue;
         const long long st = g.step[side];
+        if (!cellOk(g, c) || !cellOk(g, c - st) || !cellOk(g, c + st)) continue;
         double rec[NB], qL[N], q[N], qR[N], corr[N];
 #pragma unroll
         for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)side * NB + k) * g.V + c];
@@ -206,11 +213,13 @@ __device__ __forceinline__ void roeFluxTransformsCell(const Grid& g, const doubl
                                                       long long c, int x, int y, int z,
                                                       double* __restrict__ tape = nullptr) {
     const int N = D + 2, NB = RoeRec<D>::NB;
+    if (!cellOk(g, c)) return;
     double sR[N];
     loadState<double, D>(stage, c, sR);
 #pragma unroll
     for (int side = 0; side < D; ++side) {
         if (!roeFace(g, side, x, y, z, 2, 1)) continue;
+        if (!cellOk(g, c - g.step[side])) continue;
         double sL[N], rec[NB], corr[N], F[N];
         loadState<double, D>(stage, c - g.step[side], sL);
 #pragma unroll

@@ -150,7 +150,7 @@ __device__ __forceinline__ double* fRow(YShared& sm, int f, int r0) {
 }
 
 template <int LIM>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, 3)
     roeStageYKernel(Grid g, Phys<double> ph, int lim, const StepConst<double>* __restrict__ sc,
                     const double* __restrict__ basis, const double* __restrict__ dX, CombinePlan<double> plan,
                     const __grid_constant__ CUtensorMap tm, int loA, int hiA, unsigned* health) {

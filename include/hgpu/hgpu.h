@@ -421,6 +421,16 @@ int hgpu_checkpoint_destroy(hgpu_checkpoint* c);
  * and must be serialised by the caller.  `stream` is a cudaStream_t or NULL. */
 int hgpu_cfl_timestep_noalloc(const hgpu_config* cfg, const void* d_state, double* dt_out, void* stream);
 
+/* Checked build (the library compiled with HGPU_CHECKED, libhgpu_checked.so): every
+ * cell index a kernel computes is tested against its grid and a violation is recorded
+ * and skipped instead of trapping, and every device allocation carries guard bands of
+ * a fixed byte pattern.  Waits for the device, then returns in *flags bit 0 (an index
+ * outside a grid) and bit 1 (a guard band overwritten) since the last call, clears
+ * them, and names the first finding in hgpu_last_error.  The reference has no checks
+ * of its own (its 1D ghost kernels write out of bounds: res/Common.cl:97-194).  In
+ * the normal build: HGPU_ERR_UNSUPPORTED. */
+int hgpu_checked_status(uint32_t* flags);
+
 /* Diagnostic: measured FP64 fused multiply-add issue rate of the current device
  * (fma instructions per second, all SMs), the denominator of the FP64 roofline. */
 int hgpu_fp64_peak(double* fma_per_second);

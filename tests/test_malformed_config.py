@@ -69,3 +69,18 @@ def test_null_arguments(hg):
     c = cfg_with()
     assert hg.lib().hgpu_create(ctypes.byref(c), None) == _abi.ERR_ARG
     assert hg.lib().hgpu_set_health_mode(None, 1) == _abi.ERR_ARG
+
+
+def test_host_side_sizes_refused_before_device_work(hg):
+    """Counts and sizes the host can check are refused before any device call: an
+    empty or negative batch, and a grid beyond the allocation-free timestep's fixed
+    scratch (its pointer is never read)."""
+    h = ctypes.c_void_p()
+    arr = (_abi.HgpuConfig * 1)(cfg_with())
+    assert hg.lib().hgpu_batch_create(arr, 0, ctypes.byref(h)) == _abi.ERR_ARG
+    assert hg.lib().hgpu_batch_create(arr, -3, ctypes.byref(h)) == _abi.ERR_ARG
+    big = _abi.make_config(solver="EulerRoe", size=(4100, 4100))
+    dt = ctypes.c_double()
+    dummy = ctypes.c_double(0.)
+    assert hg.lib().hgpu_cfl_timestep_noalloc(ctypes.byref(big), ctypes.cast(ctypes.pointer(dummy), ctypes.c_void_p),
+                                              ctypes.byref(dt), None) == _abi.ERR_OOB
