@@ -35,8 +35,10 @@ namespace hgpu {
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kSegX = kThreads - 3;   // x pass: cells per segment (kSegX + 3 Delta-q-tilde faces)
+constexpr int kThreads = 256;         // y pass: threads per block
+constexpr int kThreadsX = 256;        // x pass: threads per block
+constexpr int kBlocksX = 3;           // x pass: blocks per SM the register budget is sized for
+constexpr int kSegX = kThreadsX - 3;  // x pass: cells per segment (kSegX + 3 Delta-q-tilde faces)
 constexpr int kCols = 32;             // y pass: columns per strip (one warp across)
 constexpr int kRows = kThreads / kCols;   // y pass: rows per marching step
 constexpr int kStrip = 128;           // y pass: rows per strip
@@ -45,7 +47,7 @@ static_assert(kRows == 8, "the y pass's ring indexing assumes 8 rows per step");
 
 // ---------------- x pass ----------------
 template <int LIM>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreadsX, kBlocksX)
     roeStageXKernel(Grid g, Phys<double> ph, int lim, const StepConst<double>* __restrict__ sc,
                     const double* __restrict__ stage, const double* __restrict__ basis, double* __restrict__ dX,
                     int loA, int hiA, unsigned* health) {
@@ -290,7 +292,7 @@ void launchFusedLim(const Grid& g, const Phys<double>& ph, int limiter, const St
     const int rows = g.S[1] - 4;
     const int segs = (g.S[0] - 4 + kSegX - 1) / kSegX;
     if (rows > 0 && segs > 0)
-        roeStageXKernel<LIM><<<dim3(segs, rows), kThreads, 0, st>>>(g, ph, limiter, sc, stage, basis, dX, loA, hiA,
+        roeStageXKernel<LIM><<<dim3(segs, rows), kThreadsX, 0, st>>>(g, ph, limiter, sc, stage, basis, dX, loA, hiA,
                                                                    health);
     dim3 grid((g.S[0] + kCols - 1) / kCols, (g.S[1] + kStrip - 1) / kStrip);
     roeStageYKernel<LIM><<<grid, kThreads, sizeof(YShared), st>>>(g, ph, limiter, sc, basis, dX, plan, tm, loA, hiA,
