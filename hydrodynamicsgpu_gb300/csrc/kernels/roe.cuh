@@ -191,10 +191,29 @@ __device__ __forceinline__ void rightTransformDense(const real* rec, const real*
 }
 
 // y = L x with L in the global frame: y_i = sum_j L[i][perm(j)] x_j, j ascending.
-template <typename real, int D, int SIDE>
+// FLAT: the caller's x is a difference of neighbouring states, often exactly zero.
+template <typename real, int D, int SIDE, bool FLAT = false>
 __device__ __forceinline__ void leftTransform(const real* rec, const real* x, real* y) {
     typedef RoeRec<D> R_;
     const int N = D + 2, E = N - 1;
+    // FLAT, x zero in every component (either sign) and every record entry the rows
+    // below read (VT .. LE1) finite: each product is a zero and every sum starts from
+    // +0, so y is +0 throughout.  Flat states (equal neighbours) take this exit,
+    // decided on the bit patterns, instead of N^2 zero products through the FP64 unit.
+    if (FLAT) {
+        bool flat = true;
+#pragma unroll
+        for (int j = 0; j < N; ++j) flat &= isZeroBits(x[j]);
+        if (flat) {
+#pragma unroll
+            for (int k = R_::VT; k < R_::NB; ++k) flat &= finiteBits(rec[k]);
+            if (flat) {
+#pragma unroll
+                for (int i = 0; i < N; ++i) y[i] = (real)0;
+                return;
+            }
+        }
+    }
     if (!allFinite<real, N>(x)) { leftTransformDense<real, D, SIDE>(rec, x, y); return; }
     // row 0 and row 1: dense
     {

@@ -112,7 +112,7 @@ __device__ __forceinline__ void deltaQFace(const Grid& g, const real* __restrict
     for (int k = 0; k < NB; ++k) rec[k] = basis[((long long)SIDE * NB + k) * g.V + c];
 #pragma unroll
     for (int j = 0; j < N; ++j) ds[j] = sR[j] - sL[j];
-    leftTransform<real, D, SIDE>(rec, ds, y);
+    leftTransform<real, D, SIDE, true>(rec, ds, y);
 #pragma unroll
     for (int i = 0; i < N; ++i) dq[((long long)SIDE * N + i) * g.V + c] = y[i];
 }

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kThreadsX, kBlocksX)
             for (int k = 0; k < NB; ++k) rec[k] = basis[(long long)k * g.V + c];
 #pragma unroll
             for (int j = 0; j < N; ++j) ds[j] = sS[(t + 1) * N + j] - sS[t * N + j];
-            leftTransform<double, 2, 0>(rec, ds, q);
+            leftTransform<double, 2, 0, true>(rec, ds, q);
         }
 #pragma unroll
         for (int j = 0; j < N; ++j) sQ[t * N + j] = q[j];
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kThreads, 3)
             const double* sL = yRow(sm, f - 1, r0) + tx * N;
 #pragma unroll
             for (int j = 0; j < N; ++j) ds[j] = sR[j] - sL[j];
-            leftTransform<double, 2, 1>(rec, ds, q);
+            leftTransform<double, 2, 1, true>(rec, ds, q);
         }
         double* o = qRow(sm, f, r0) + tx * N;
 #pragma unroll
