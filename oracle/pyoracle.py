@@ -90,8 +90,32 @@ def max_threads():
     return lib().oracle_max_threads()
 
 
+# Grids below this many cells run single-threaded: an OpenMP parallel region per kernel
+# costs more than the work of a small grid (and far more on a loaded machine).
+SMALL_GRID_CELLS = 1 << 16
+
+
+class _OneThread:
+    """Context: the library's OpenMP thread count is 1 inside, restored after."""
+
+    def __init__(self, get, put, active):
+        self.get, self.put, self.active = get, put, active
+
+    def __enter__(self):
+        if self.active:
+            self.prev = self.get()
+            self.put(1)
+
+    def __exit__(self, *exc):
+        if self.active:
+            self.put(self.prev)
+
+
 class _Base:
     dtype = np.float64
+
+    def _small(self):
+        return _abi.config_volume(self.cfg) < SMALL_GRID_CELLS
 
     def _np(self):
         return np.float32 if self.cfg.precision == _abi.FP32 else np.float64
@@ -127,12 +151,16 @@ class Oracle(_Base):
     def set_state(self, a, potential=None):
         a = np.ascontiguousarray(a, dtype=self._np()).reshape(-1)
         assert a.size == self.count
-        if potential is None:
-            st = lib().oracle_set_state(self.h, a.ctypes.data, a.size)
-        else:
-            p = np.ascontiguousarray(potential, dtype=self._np()).reshape(-1)
-            st = lib().oracle_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size)
+        with self._threads():
+            if potential is None:
+                st = lib().oracle_set_state(self.h, a.ctypes.data, a.size)
+            else:
+                p = np.ascontiguousarray(potential, dtype=self._np()).reshape(-1)
+                st = lib().oracle_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size)
         assert st == 0
+
+    def _threads(self):
+        return _OneThread(lib().oracle_max_threads, lib().oracle_set_threads, self._small())
 
     def get_potential(self):
         a = np.empty(_abi.config_volume(self.cfg), dtype=self._np())
@@ -148,7 +176,8 @@ class Oracle(_Base):
     def update(self, nsteps=1):
         dt = ctypes.c_double()
         bad = ctypes.c_int()
-        lib().oracle_update(self.h, int(nsteps), ctypes.byref(dt), ctypes.byref(bad))
+        with self._threads():
+            lib().oracle_update(self.h, int(nsteps), ctypes.byref(dt), ctypes.byref(bad))
         self.last_dt = dt.value
         self.nonfinite = bool(bad.value)
         return dt.value
@@ -231,13 +260,17 @@ class Refcl(_Base):
             self.L.refcl_destroy(self.h)
             self.h = None
 
+    def _threads(self):
+        return _OneThread(self.L.refcl_max_threads, self.L.refcl_set_threads, self._small())
+
     def set_state(self, a, potential=None):
         a = np.ascontiguousarray(a, dtype=self._np()).reshape(-1)
-        if potential is None:
-            assert self.L.refcl_set_state(self.h, a.ctypes.data, a.size) == 0
-        else:
-            p = np.ascontiguousarray(potential, dtype=self._np()).reshape(-1)
-            assert self.L.refcl_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size) == 0
+        with self._threads():
+            if potential is None:
+                assert self.L.refcl_set_state(self.h, a.ctypes.data, a.size) == 0
+            else:
+                p = np.ascontiguousarray(potential, dtype=self._np()).reshape(-1)
+                assert self.L.refcl_set_state_potential(self.h, a.ctypes.data, a.size, p.ctypes.data, p.size) == 0
 
     def get_potential(self):
         a = np.empty(_abi.config_volume(self.cfg), dtype=self._np())
@@ -251,7 +284,8 @@ class Refcl(_Base):
 
     def update(self, nsteps=1):
         dt = ctypes.c_double()
-        self.L.refcl_update(self.h, int(nsteps), ctypes.byref(dt))
+        with self._threads():
+            self.L.refcl_update(self.h, int(nsteps), ctypes.byref(dt))
         self.last_dt = dt.value
         return dt.value
 
