@@ -542,9 +542,10 @@ def fp64_roofline(prof, value, fp64_peak):
     return per_update, achieved, achieved / fp64_peak
 
 
-def summary_block(value, e2e, roofline, batched, adjoint):
+def summary_block(value, e2e, roofline, batched, adjoint, fused=None):
     """The headline numbers in a few keys, placed last in the JSON line."""
     out = {"value": value, "e2e": e2e["value"] if e2e else None,
+           "fused_stage_ms_per_step": fused["ms_per_step"] if fused else None,
            "fp64_frac": roofline["frac"], "hbm_frac_dominant_kernel": roofline["hbm"]["frac"],
            "hbm_frac_step": roofline["hbm_step"]["frac"]}
     if batched:
@@ -635,6 +636,19 @@ def run_gb300(args):
     breakdown = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / sum(x[1] for x in prof.values())}
                  for k, v in prof.items()}
 
+    # ---- the same step with each stage as the two fused per-direction kernels (opt-in
+    # path, hgpu_set_fused_stages; same bits) ----
+    fused = None
+    if rank == 0 and world == 1:
+        fs = hg.Solver(cfg)
+        fs.set_fused_stages(True)
+        fs.resetState(init)
+        fs.update(args.warmup, want_dt=False)
+        fms = fs.timed_update(args.steps) / args.steps
+        fs.close()
+        fused = {"ms_per_step": fms, "value": interior / (fms * 1e-3), "unit": UNIT,
+                 "vs_default": ms_per_step / fms, "kernels": "x pass + y pass per stage (roe_fused.cu)"}
+
     # ---- e2e through the C ABI: hgpu_update_host per step = H2D from pinned host, the
     # step, D2H to pinned host and the dt read, the copies overlapped in bands ----
     e2e = None
@@ -690,12 +704,13 @@ def run_gb300(args):
         "e2e": e2e,
         "clocks": clk,
         "fp32": fp32,
+        "fused_stage": fused,
         "self_gravity": gravity,
         "adjoint": adjoint,
         "batched_sweep": batched,
         "gpu_launches": kernels_per_step * args.steps,
         "health_flags": health,
-        "summary": summary_block(value, e2e, roofline, batched, adjoint),
+        "summary": summary_block(value, e2e, roofline, batched, adjoint, fused),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

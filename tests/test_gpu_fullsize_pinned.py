@@ -50,14 +50,18 @@ def make_cfg(fx):
     return _abi.make_config(**kw)
 
 
-@pytest.mark.parametrize("name", NAMES)
-def test_full_length_run_matches_reference_kernels(hg, name):
+@pytest.mark.parametrize("name,fused", [(n, False) for n in NAMES] + [(NAMES[0], True)])
+def test_full_length_run_matches_reference_kernels(hg, name, fused):
+    """fused: the same run with each Runge-Kutta stage as the two fused per-direction
+    kernels (hgpu_set_fused_stages)."""
     fx = load(name)
     init = make_init(fx)
     assert state_digest(init) == fx["init_sha256"], \
         "the initial-condition generator gives a different state on this platform"
     s = hg.Solver(make_cfg(fx))
     try:
+        if fused:
+            s.set_fused_stages(True)
         s.resetState(init)
         for k in range(1, fx["steps"] + 1):
             dt = s.update(1)
