@@ -60,6 +60,7 @@ SIGNATURES = {
     "hgpu_update_frozen_dt": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_double]),
     "hgpu_checkpoint_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "hgpu_checkpoint_create_taped": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P)]),
     "hgpu_checkpoint_forward": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "hgpu_checkpoint_dts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "hgpu_checkpoint_backward": (ctypes.c_int, [_P, _P, _P]),
@@ -458,9 +459,14 @@ class Checkpoints:
     (hgpu_checkpoint_*): forward() keeps every `every`-th state and each step's dt,
     backward() maps the cotangent of the final state to that of the initial state."""
 
-    def __init__(self, solver, nsteps, every):
+    def __init__(self, solver, nsteps, every=None, taped=False):
+        """taped: record every step's tape during forward() (hgpu_checkpoint_create_taped;
+        memory for nsteps tapes), so backward() runs the reverse steps only."""
         h = ctypes.c_void_p()
-        check(lib().hgpu_checkpoint_create(solver.h, int(nsteps), int(every), ctypes.byref(h)))
+        if taped:
+            check(lib().hgpu_checkpoint_create_taped(solver.h, int(nsteps), ctypes.byref(h)))
+        else:
+            check(lib().hgpu_checkpoint_create(solver.h, int(nsteps), int(every), ctypes.byref(h)))
         self.h, self.solver, self.nsteps = h, solver, int(nsteps)
 
     def close(self):

@@ -10,10 +10,17 @@
 
 namespace hgpu {
 
+static const unsigned long long kAccInf = 0x7FF0000000000000ULL;   // the bits of +Inf
+
 RoeAdjoint::RoeAdjoint(const ResolvedConfig& rc, cudaStream_t stream) : rc_(rc), stream_(stream) {
     rc_.grid.check = checkWord();
     if (rc.cfg.solver != HGPU_SOLVER_ROE || rc.cfg.precision != HGPU_FP64 || rc.cfg.compat != HGPU_COMPAT_REF)
         throw ConfigError(HGPU_ERR_UNSUPPORTED, "the adjoint covers EulerRoe in FP64 with the REF scheme");
+    // with useFixedDT, Solver::update never calls calcTimestep, so EulerRoe steps with the
+    // eigenbasis buffer as the last CFL step (or the allocation) left it
+    // (src/Solver/Solver.cpp:521-535, src/Solver/Roe.cpp:82-92): not the step differentiated here
+    if (rc.cfg.use_fixed_dt)
+        throw ConfigError(HGPU_ERR_UNSUPPORTED, "the adjoint differentiates the CFL-dt step (use_fixed_dt = 0)");
     for (int i = 0; i < 3; ++i) {
         ph_.dx[i] = rc.dx[i];
         ph_.rdx[i] = 1. / ph_.dx[i];
@@ -29,6 +36,10 @@ RoeAdjoint::RoeAdjoint(const ResolvedConfig& rc, cudaStream_t stream) : rc_(rc),
     flux_ = DeviceBuffer(sizeof(double) * V * N * D, true);
     sc_ = DeviceBuffer(sizeof(StepConst<double>), true);
     acc_ = DeviceBuffer(sizeof(unsigned long long), true);
+    {   // the CFL minimum starts from +Inf (every Roe dtBuffer entry is written, Solver.cpp:217-222)
+        const unsigned long long inf = kAccInf;
+        cudaCheck(cudaMemcpy(acc_.get(), &inf, sizeof inf, cudaMemcpyHostToDevice), "dt accumulator init");
+    }
     health_ = DeviceBuffer(sizeof(unsigned), true);
     lamTmp_ = DeviceBuffer(sizeof(double) * V * N, true);
     if (!fe_) {
@@ -72,7 +83,7 @@ size_t RoeAdjoint::tapeBytes() const {
     return sizeof(double) * V * (D * roeRecordSize((int)D) + stages_ * (N + N * D + roeFluxTapePlanes((int)D)));
 }
 
-void RoeAdjoint::forward(const double* u_n, double dt, Tape& t, double* u_next) {
+void RoeAdjoint::forward(const double* u_n, double dt, Tape& t, double* u_next, double* dtOut) {
     const Grid& g = rc_.grid;
     const size_t bytes = sizeof(double) * (size_t)g.V * rc_.numStates;
     double* cur = cur_.as<double>();
@@ -80,7 +91,16 @@ void RoeAdjoint::forward(const double* u_n, double dt, Tape& t, double* u_next) 
     if (u_n != cur) cudaCheck(cudaMemcpyAsync(cur, u_n, bytes, cudaMemcpyDeviceToDevice, stream_), "adjoint input");
     launchBoundary<double>(g, methods_, cur, stream_);
     launchRoeBasis<double>(g, ph_, cur, t.basis.as<double>(), 0, stream_);
-    launchFinalizeDt<double>(ph_, integ_, 1, dt, acc_.as<unsigned long long>(), 0, sc, health_.as<unsigned>(), stream_);
+    if (dtOut) {                                   // Solver::update's CFL dt
+        launchRoeDt<double>(g, ph_, t.basis.as<double>(), acc_.as<unsigned long long>(), health_.as<unsigned>(),
+                            stream_);
+        launchFinalizeDt<double>(ph_, integ_, 0, 0., acc_.as<unsigned long long>(), kAccInf, sc,
+                                 health_.as<unsigned>(), stream_);
+        cudaCheck(cudaMemcpyAsync(dtOut, &sc->dt_f64, sizeof(double), cudaMemcpyDeviceToDevice, stream_), "record dt");
+    } else {
+        launchFinalizeDt<double>(ph_, integ_, 1, dt, acc_.as<unsigned long long>(), 0, sc, health_.as<unsigned>(),
+                                 stream_);
+    }
     auto stage = [&](int k, const double* in) {
         cudaCheck(cudaMemcpyAsync(t.U[k].get(), in, bytes, cudaMemcpyDeviceToDevice, stream_), "tape stage");
         launchRoeDeltaQ<double>(g, in, t.basis.as<double>(), t.DQ[k].as<double>(), 0, stream_);
@@ -149,17 +169,23 @@ void RoeAdjoint::step(const double* u_n, const double* lamNext, double* lamOut, 
 
 // ---------------- checkpoints ----------------
 Checkpoints::Checkpoints(RoeAdjoint* adj, double* state, cudaStream_t stream, int nsteps, int every,
-                         std::function<void()> cflStep, const double* cflDt)
-    : adj_(adj), state_(state), stream_(stream), nsteps_(nsteps), every_(every), cflStep_(std::move(cflStep)),
-      cflDt_(cflDt) {
+                         std::function<void()> cflStep, const double* cflDt, bool taped)
+    : adj_(adj), state_(state), stream_(stream), nsteps_(nsteps), every_(every), taped_(taped),
+      cflStep_(std::move(cflStep)), cflDt_(cflDt) {
     if (nsteps < 1 || every < 1) throw ConfigError(HGPU_ERR_ARG, "nsteps and checkpoint interval must be positive");
-    every_ = std::min(every, nsteps);
+    every_ = taped ? nsteps : std::min(every, nsteps);
     const auto& rc = adj->config();
     const size_t bytes = sizeof(double) * (size_t)rc.grid.V * rc.numStates;
-    for (int i = 0; i < (nsteps + every_ - 1) / every_; ++i) ckpt_.emplace_back(bytes, false);
+    if (taped) {   // refuse before allocating what the device cannot hold
+        size_t freeB = 0, totalB = 0;
+        cudaCheck(cudaMemGetInfo(&freeB, &totalB), "cudaMemGetInfo");
+        if ((double)adj->tapeBytes() * nsteps > 0.95 * (double)freeB)
+            throw ConfigError(HGPU_ERR_NOMEM, "the tapes of every step do not fit in device memory");
+    } else {
+        for (int i = 0; i < (nsteps + every_ - 1) / every_; ++i) ckpt_.emplace_back(bytes, false);
+    }
     for (int i = 0; i < every_; ++i) tapes_.push_back(adj->makeTape());
     dtDev_ = DeviceBuffer(sizeof(double) * nsteps, true);
-    next_ = DeviceBuffer(bytes, false);
     lamA_ = DeviceBuffer(bytes, false);
     lamB_ = DeviceBuffer(bytes, false);
     dts.assign(nsteps, 0.);
@@ -176,7 +202,16 @@ void Checkpoints::forward(const double* dtsIn) {
     const auto& rc = adj_->config();
     const size_t bytes = sizeof(double) * (size_t)rc.grid.V * rc.numStates;
     cudaCheck(cudaEventRecord(e0_, stream_), "event");
-    for (int i = 0; i < nsteps_; ++i) {
+    if (taped_) {                                   // every step records its own tape
+        const double* u = state_;
+        for (int i = 0; i < nsteps_; ++i) {
+            if (dtsIn) dts[i] = dtsIn[i];
+            adj_->forward(u, dtsIn ? dtsIn[i] : 0., tapes_[i], nullptr, dtsIn ? nullptr : dtDev_.as<double>() + i);
+            u = adj_->work();
+        }
+        cudaCheck(cudaMemcpyAsync(state_, u, bytes, cudaMemcpyDeviceToDevice, stream_), "final state");
+    }
+    for (int i = 0; i < nsteps_ && !taped_; ++i) {
         if (i % every_ == 0)
             cudaCheck(cudaMemcpyAsync(ckpt_[i / every_].get(), state_, bytes, cudaMemcpyDeviceToDevice, stream_),
                       "checkpoint");
@@ -210,10 +245,10 @@ void Checkpoints::backward(const double* lamT, double* lam0) {
     const int nseg = (nsteps_ + every_ - 1) / every_;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int first = seg * every_, last = std::min(nsteps_, first + every_);
-        const double* u = ckpt_[seg].as<double>();
-        for (int j = first; j < last; ++j) {                       // recompute, recording tapes
-            adj_->forward(u, dts[j], tapes_[j - first], next_.as<double>());
-            u = next_.as<double>();
+        const double* u = taped_ ? nullptr : ckpt_[seg].as<double>();
+        for (int j = first; j < last && !taped_; ++j) {            // recompute, recording tapes, on
+            adj_->forward(u, dts[j], tapes_[j - first], nullptr);  // the adjoint's working state
+            u = adj_->work();
         }
         for (int j = last - 1; j >= first; --j) {                  // reverse steps
             adj_->reverse(tapes_[j - first], dts[j], lam, other);

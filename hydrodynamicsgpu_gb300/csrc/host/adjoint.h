@@ -22,8 +22,12 @@ public:
     };
     RoeAdjoint(const ResolvedConfig& rc, cudaStream_t stream);
     Tape makeTape() const;
-    // u_next = step(u_n; dt) (u_next may be u_n or null); records `t`
-    void forward(const double* u_n, double dt, Tape& t, double* u_next);
+    // u_next = step(u_n; dt) (u_next may be u_n or null); records `t`.  The step runs
+    // on the working state (work()): u_n == work() and u_next == null skip both copies.
+    // With dtOut (a device double) the step takes the CFL dt of u_n, as Solver::update
+    // does, and writes it there; `dt` is then unused.
+    void forward(const double* u_n, double dt, Tape& t, double* u_next, double* dtOut = nullptr);
+    const double* work() const { return cur_.as<double>(); }
     // lamOut = (d u^{n+1} / d u^n)^T lamNext for the step recorded in `t` (lamOut != lamNext)
     void reverse(const Tape& t, double dt, const double* lamNext, double* lamOut);
     // state <- step(state; dt) (no tape kept beyond this call)
@@ -51,10 +55,13 @@ private:
 // Checkpointed trajectory: the forward keeps the state every `every` steps and the dt
 // of every step; the backward recomputes one segment at a time (recording its tapes)
 // and runs the reverse steps, so memory is (nsteps/every) states + `every` tapes.
+// Taped: the forward records every step's tape as it goes (the adjoint's recording
+// step, the same kernels as Solver::update), and the backward runs the reverse steps
+// only; memory is nsteps tapes (tapeBytes() each).
 class Checkpoints {
 public:
     Checkpoints(RoeAdjoint* adj, double* state, cudaStream_t stream, int nsteps, int every,
-                std::function<void()> cflStep, const double* cflDt);
+                std::function<void()> cflStep, const double* cflDt, bool taped = false);
     void forward(const double* dts);                         // host dts or null (CFL)
     void backward(const double* lamT, double* lam0);        // device arrays
     std::vector<double> dts;
@@ -65,11 +72,12 @@ private:
     double* state_;
     cudaStream_t stream_;
     int nsteps_, every_;
+    bool taped_;
     std::function<void()> cflStep_;
     const double* cflDt_;
     std::vector<DeviceBuffer> ckpt_;
     std::vector<RoeAdjoint::Tape> tapes_;
-    DeviceBuffer dtDev_, next_, lamA_, lamB_;
+    DeviceBuffer dtDev_, lamA_, lamB_;
     cudaEvent_t e0_ = nullptr, e1_ = nullptr;
     bool forwardDone_ = false;
 public:

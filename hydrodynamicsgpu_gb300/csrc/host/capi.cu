@@ -451,7 +451,7 @@ int hgpu_adjoint_step(hgpu_solver* h, const void* d_u_n, const void* d_lambda_ne
     });
 }
 
-int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoint** out) {
+static int createCheckpoints(hgpu_solver* h, int nsteps, int every, bool taped, hgpu_checkpoint** out) {
     if (!h || !out || nsteps < 1 || every < 1) return fail(HGPU_ERR_ARG, "bad argument");
     *out = nullptr;
     return guarded([&]() {
@@ -460,11 +460,19 @@ int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoin
         std::unique_ptr<hgpu_checkpoint> c(new hgpu_checkpoint());
         c->h = h;
         c->c.reset(new hgpu::Checkpoints(&a, s->state.as<double>(), s->stream, nsteps, every,
-                                         [h]() { runSteps(h, 1); }, &s->sc()->dt_f64));
+                                         [h]() { runSteps(h, 1); }, &s->sc()->dt_f64, taped));
         h->checkpoints.push_back(c.get());
         *out = c.release();
         return (int)HGPU_OK;
     });
+}
+
+int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoint** out) {
+    return createCheckpoints(h, nsteps, every, false, out);
+}
+
+int hgpu_checkpoint_create_taped(hgpu_solver* h, int nsteps, hgpu_checkpoint** out) {
+    return createCheckpoints(h, nsteps, nsteps, true, out);
 }
 
 int hgpu_checkpoint_forward(hgpu_checkpoint* c, const double* dts) {

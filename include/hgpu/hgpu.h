@@ -394,6 +394,12 @@ int hgpu_adjoint_step(hgpu_solver* h, const void* d_u_n, const void* d_lambda_ne
  * recomputes one segment at a time and runs its reverse steps. */
 typedef struct hgpu_checkpoint hgpu_checkpoint;
 int hgpu_checkpoint_create(hgpu_solver* h, int nsteps, int every, hgpu_checkpoint** out);
+/* The same trajectory with every step's tape recorded during the forward (the
+ * adjoint's recording step: the same kernels and dt as hgpu_update), so the backward
+ * runs the reverse steps only.  Memory: nsteps tapes (about 40 doubles per cell and
+ * stage for 2D RK); HGPU_ERR_NOMEM when they do not fit.  The forward leaves the
+ * final state in the solver like the checkpointed one (it runs no state check). */
+int hgpu_checkpoint_create_taped(hgpu_solver* h, int nsteps, hgpu_checkpoint** out);
 /* dts: nsteps frozen values, or NULL for the CFL dt of each step (recorded). */
 int hgpu_checkpoint_forward(hgpu_checkpoint* c, const double* dts);
 int hgpu_checkpoint_dts(hgpu_checkpoint* c, double* dts, int n);

@@ -200,6 +200,65 @@ def test_checkpointed_gradient(hg, oracle_mod, every):
     s.close()
 
 
+def run_trajectory(hg, cfg, u0, nsteps, every=None, taped=False, dts=None):
+    """final state, dts and lambda_0 of a density loss through nsteps steps"""
+    s = hg.Solver(cfg)
+    try:
+        s.resetState(u0)
+        cp = hg.Checkpoints(s, nsteps, every, taped=taped)
+        cp.forward(dts)
+        d = cp.dts()
+        uT = s.getState().copy()
+        target = uT + 1e-2 * np.random.default_rng(201).standard_normal(uT.size) * np.abs(uT)
+        _, lamT = density_loss_cotangent(cfg, uT, target)
+        dl = cuda(lamT)
+        out = torch.empty_like(dl)
+        torch.cuda.synchronize()
+        cp.backward(dl.data_ptr(), out.data_ptr())
+        s.synchronize()
+        g = out.cpu().numpy()
+        cp.close()
+        return uT, d, g
+    finally:
+        s.close()
+
+
+@pytest.mark.parametrize("integrator,frozen", [("RungeKutta2", False), ("RungeKutta4", False), ("ForwardEuler", False),
+                                               ("RungeKutta3TVD", False), ("RungeKutta2Heun", True)])
+def test_taped_trajectory_equals_checkpointed(hg, integrator, frozen):
+    """The taped forward (every step's tape recorded as it runs, CFL dt taken on the
+    device) gives the checkpointed forward's states, dts and gradient bit for bit, and
+    its final state is the plain solver's."""
+    cfg, u0 = kh_small(n=20, seed=103)
+    cfg.integrator = _abi.INTEGRATORS.index(integrator)
+    nsteps = 12
+    dts = None
+    if frozen:
+        dts = np.array(run_trajectory(hg, cfg, u0, nsteps, every=5)[1]) * .9
+    uA, dA, gA = run_trajectory(hg, cfg, u0, nsteps, every=5, dts=dts)
+    uB, dB, gB = run_trajectory(hg, cfg, u0, nsteps, taped=True, dts=dts)
+    assert np.array_equal(dA, dB)
+    assert np.array_equal(uA, uB)
+    assert np.array_equal(gA, gB)
+    if not frozen:
+        s = hg.Solver(cfg)
+        s.resetState(u0)
+        s.update(nsteps)
+        assert np.array_equal(s.getState(), uB)
+        s.close()
+
+
+def test_taped_refuses_what_does_not_fit(hg):
+    cfg, u0 = kh_small(n=508)
+    s = hg.Solver(cfg)
+    try:
+        s.resetState(u0)
+        with pytest.raises(hg.HgpuError):
+            hg.Checkpoints(s, 1 << 20, taped=True)      # a million tapes of a 512^2 grid
+    finally:
+        s.close()
+
+
 def drifting_flow(n=32, limiter="VanAlbada1"):
     """Smooth periodic flow whose velocities stay away from zero (u ~ .4, v ~ .3):
     no face changes its upwind side and VanAlbada1 has no kinks, so the rollout is
@@ -280,3 +339,22 @@ def test_adjoint_rejects_other_solvers(hg):
     with pytest.raises(hg.HgpuError):
         s.update_frozen_dt([1e-3])
     s.close()
+
+
+def test_adjoint_rejects_fixed_dt(hg):
+    """With useFixedDT an EulerRoe step keeps the eigenbasis the last CFL step left
+    (Solver::update skips calcTimestep): the adjoint refuses such a solver."""
+    cfg, u0 = kh_small()
+    cfg.use_fixed_dt = 1
+    cfg.fixed_dt = .001
+    s = hg.Solver(cfg)
+    try:
+        s.resetState(u0)
+        with pytest.raises(hg.HgpuError):
+            hg.Checkpoints(s, 4, 2)
+        with pytest.raises(hg.HgpuError):
+            hg.Checkpoints(s, 4, taped=True)
+        with pytest.raises(hg.HgpuError):
+            s.update_frozen_dt([1e-3])
+    finally:
+        s.close()
