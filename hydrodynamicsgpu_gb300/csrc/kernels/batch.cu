@@ -38,37 +38,38 @@ __global__ void __launch_bounds__(256) batchBoundaryKernel(const BatchProblem<re
     }
 }
 
-template <typename real, int D>
+template <typename real, int D, bool PLAIN>
 __global__ void __launch_bounds__(256) batchRoeBasisKernel(const BatchProblem<real>* __restrict__ P,
                                                            const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                            int loA, int hiA, const real* __restrict__ state,
                                                            real* __restrict__ basis, unsigned* q) {
     extern __shared__ unsigned char smem[];
     RoePrim<real, D>* prim = reinterpret_cast<RoePrim<real, D>*>(smem);
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
+        const Grid g = pr.g;
         const real* s = state + (long long)(D + 2) * pr.stateOff;
         real* b = basis + pr.faceOff;
         if (tu.staged) {
-            roeBasisTile<real, D>(pr.g, pr.ph, s, b, loA, hiA, tl.x0, tl.y0, tl.z0, tu.tx, tu.ty, tu.tz, prim);
+            roeBasisTile<real, D>(g, pr.ph, s, b, loA, hiA, tl.x0, tl.y0, tl.z0, tu.tx, tu.ty, tu.tz, prim);
         } else {
-            for (int r = 0; r < tu.cpt; ++r) {
+            for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r) {
             int x, y, z;
             long long c;
-            if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) {
+            if (tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) {
                 const int NB = RoeRec<D>::NB;
                 real sR[D + 2], sL[D + 2], rec[NB];
                 loadState<real, D>(s, c, sR);
 #pragma unroll
                 for (int side = 0; side < D; ++side) {
-                    if (!roeFace(pr.g, side, x, y, z, loA, hiA)) continue;
-                    loadState<real, D>(s, c - pr.g.step[side], sL);
+                    if (!roeFace(g, side, x, y, z, loA, hiA)) continue;
+                    loadState<real, D>(s, c - g.step[side], sL);
                     if (side == 0) roeBasis<real, D, 0>(sL, sR, pr.ph.gamma, rec);
                     else if (side == 1) roeBasis<real, D, (D > 1 ? 1 : 0)>(sL, sR, pr.ph.gamma, rec);
                     else roeBasis<real, D, (D > 2 ? 2 : 0)>(sL, sR, pr.ph.gamma, rec);
 #pragma unroll
-                    for (int k = 0; k < NB; ++k) b[((long long)side * NB + k) * pr.g.V + c] = rec[k];
+                    for (int k = 0; k < NB; ++k) b[((long long)side * NB + k) * g.V + c] = rec[k];
                 }
             }
             }
@@ -108,37 +109,39 @@ __global__ void batchFinalizeKernel(const BatchProblem<real>* __restrict__ P, in
     finalizeOne<real>(pr.ph, integ, pr.useFixed, pr.fixedDt, acc + p, pr.accInit, sc + p);
 }
 
-template <typename real, int D>
+template <typename real, int D, bool PLAIN>
 __global__ void __launch_bounds__(256) batchDeltaQKernel(const BatchProblem<real>* __restrict__ P,
                                                          const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                          int loA, int hiA, const real* __restrict__ stage,
                                                          const real* __restrict__ basis, real* __restrict__ dq,
                                                          unsigned* q) {
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
+        const Grid g = pr.g;
         int x, y, z;
         long long c;
-        for (int r = 0; r < tu.cpt; ++r)
-        if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
-            roeDeltaQCell<real, D>(pr.g, stage + (long long)(D + 2) * pr.stateOff, basis + pr.faceOff, dq + pr.dqOff, c,
+        for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r)
+        if (tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
+            roeDeltaQCell<real, D>(g, stage + (long long)(D + 2) * pr.stateOff, basis + pr.faceOff, dq + pr.dqOff, c,
                                    x, y, z, loA, hiA);
     }
 }
 
-template <typename real, int D>
+template <typename real, int D, bool PLAIN>
 __global__ void __launch_bounds__(256) batchCombineKernel(const BatchProblem<real>* __restrict__ P,
                                                           const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                           const real* __restrict__ flux, CombinePlan<real> plan,
                                                           const StepConst<real>* __restrict__ sc, unsigned* q) {
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
+        const Grid g = pr.g;
         int x, y, z;
         long long c;
-        for (int r = 0; r < tu.cpt; ++r)
-        if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
-            derivCombineCell<real, D, D>(pr.g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
+        for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r)
+        if (tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
+            derivCombineCell<real, D, D>(g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
     }
 }
 
@@ -224,11 +227,15 @@ template <typename real>
 void BatchLaunch<real>::roeBasis(int loA, int hiA, unsigned* q) const {
     int smem = tu.staged ? primSmem<real>(dim, tu) : 0;
 #define L(DD)                                                                                                      \
-    batchRoeBasisKernel<real, DD><<<persistentBlocks(batchRoeBasisKernel<real, DD>, smem, tu.blocksPerSM, nT), 256, smem, \
-                                    st>>>(P, tiles, nT, tu, loA, hiA, state, faces, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
+    if (tu.blocksPerSM < 0 && tu.cpt == 1)                                                                                        \
+        batchRoeBasisKernel<real, DD, true><<<nT, 256, smem, st>>>(P, tiles, nT, tu, loA, hiA, state, faces, q);    \
+    else                                                                                                           \
+        batchRoeBasisKernel<real, DD, false><<<persistentBlocks(batchRoeBasisKernel<real, DD, false>, smem,         \
+                                                                tu.blocksPerSM, nT), 256, smem, st>>>(              \
+            P, tiles, nT, tu, loA, hiA, state, faces, q)
+    if (dim == 1) { L(1); }
+    else if (dim == 2) { L(2); }
+    else { L(3); }
 #undef L
 }
 
@@ -263,20 +270,32 @@ void BatchLaunch<real>::finalize(int integ, unsigned long long* acc, StepConst<r
 
 template <typename real>
 void BatchLaunch<real>::deltaQ(int loA, int hiA, const real* stage, real* dq, unsigned* q) const {
-#define L(DD) batchDeltaQKernel<real, DD><<<persistentBlocks(batchDeltaQKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, loA, hiA, stage, faces, dq, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
+#define L(DD)                                                                                                      \
+    if (tu.blocksPerSM < 0 && tu.cpt == 1)                                                                                        \
+        batchDeltaQKernel<real, DD, true><<<nT, 256, 0, st>>>(P, tiles, nT, tu, loA, hiA, stage, faces, dq, q);     \
+    else                                                                                                           \
+        batchDeltaQKernel<real, DD, false><<<persistentBlocks(batchDeltaQKernel<real, DD, false>, 0, tu.blocksPerSM, \
+                                                              nT), 256, 0, st>>>(P, tiles, nT, tu, loA, hiA, stage,  \
+                                                                                 faces, dq, q)
+    if (dim == 1) { L(1); }
+    else if (dim == 2) { L(2); }
+    else { L(3); }
 #undef L
 }
 
 template <typename real>
 void BatchLaunch<real>::combine(const real* fluxBuf, const CombinePlan<real>& plan, const StepConst<real>* sc,
                                 unsigned* q) const {
-#define L(DD) batchCombineKernel<real, DD><<<persistentBlocks(batchCombineKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, fluxBuf, plan, sc, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
+#define L(DD)                                                                                                      \
+    if (tu.blocksPerSM < 0 && tu.cpt == 1)                                                                                        \
+        batchCombineKernel<real, DD, true><<<nT, 256, 0, st>>>(P, tiles, nT, tu, fluxBuf, plan, sc, q);             \
+    else                                                                                                           \
+        batchCombineKernel<real, DD, false><<<persistentBlocks(batchCombineKernel<real, DD, false>, 0,              \
+                                                               tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu,  \
+                                                                                                  fluxBuf, plan, sc, q)
+    if (dim == 1) { L(1); }
+    else if (dim == 2) { L(2); }
+    else { L(3); }
 #undef L
 }
 

@@ -44,41 +44,44 @@ __global__ void __launch_bounds__(256) batchFluxKernel(const BatchProblem<real>*
 // The FP64 EulerRoe flux in the single-problem kernels' two passes (roe_cells.cuh):
 // per-wave corrections into the flux buffer, then the transforms over them.  Fewer
 // live registers than the one-pass body, the same bits.
-template <int D, int LIM>
+template <int D, int LIM, bool PLAIN>
 __global__ void __launch_bounds__(256) batchFluxCorrKernel(const BatchProblem<double>* __restrict__ P,
                                                            const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                            int lim, const StepConst<double>* __restrict__ sc,
                                                            const double* __restrict__ faces,
                                                            const double* __restrict__ dq, double* __restrict__ flux,
                                                            unsigned* q) {
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<double>& pr = P[tl.p];
-        for (int r = 0; r < tu.cpt; ++r) {
+        const Grid g = pr.g;
+        for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r) {
             int x, y, z;
             long long c;
-            if (!tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
-            roeFluxCorrectionsCell<D, LIM>(pr.g, lim, sc[tl.p], faces + pr.faceOff, dq + pr.dqOff, flux + pr.dqOff, c,
-                                           x, y, z);
+            if (!tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
+            roeFluxCorrectionsCell<D, LIM>(g, lim, sc[tl.p], faces + pr.faceOff, dq + pr.dqOff, flux + pr.dqOff, c, x,
+                                           y, z);
         }
     }
 }
 
-template <int D>
-__global__ void __launch_bounds__(256) batchFluxXformKernel(const BatchProblem<double>* __restrict__ P,
+// (2D plain: capped at 3 blocks per SM, 80 registers with a few spilled, as measured faster)
+template <int D, bool PLAIN>
+__global__ void __launch_bounds__(256, PLAIN && D <= 2 ? 3 : 1) batchFluxXformKernel(const BatchProblem<double>* __restrict__ P,
                                                             const BatchTile* __restrict__ tiles, int nT, BatchTuning tu,
                                                             const double* __restrict__ stage,
                                                             const double* __restrict__ faces,
                                                             double* __restrict__ flux, unsigned* q) {
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<double>& pr = P[tl.p];
-        for (int r = 0; r < tu.cpt; ++r) {
+        const Grid g = pr.g;
+        for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r) {
             int x, y, z;
             long long c;
-            if (!tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
-            roeFluxTransformsCell<D>(pr.g, stage + (long long)(D + 2) * pr.stateOff, faces + pr.faceOff,
-                                     flux + pr.dqOff, c, x, y, z);
+            if (!tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
+            roeFluxTransformsCell<D>(g, stage + (long long)(D + 2) * pr.stateOff, faces + pr.faceOff, flux + pr.dqOff,
+                                     c, x, y, z);
         }
     }
 }
@@ -117,10 +120,16 @@ static void batchFluxSplitLaunch(const BatchProblem<double>* P, const BatchTile*
                                  int dim, cudaStream_t st, const double* faces, int lim, const StepConst<double>* sc,
                                  const double* stage, const double* dq, double* fluxBuf, unsigned* q0, unsigned* q1) {
 #define L(DD)                                                                                                       \
-    batchFluxCorrKernel<DD, LIM><<<persistentBlocks(batchFluxCorrKernel<DD, LIM>, 0, tu.blocksPerSM, nT), 256, 0, st>>>( \
-        P, tiles, nT, tu, lim, sc, faces, dq, fluxBuf, q0);                                                         \
-    batchFluxXformKernel<DD><<<persistentBlocks(batchFluxXformKernel<DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(       \
-        P, tiles, nT, tu, stage, faces, fluxBuf, q1)
+    if (tu.blocksPerSM < 0 && tu.cpt == 1) {                                                                                       \
+        batchFluxCorrKernel<DD, LIM, true><<<nT, 256, 0, st>>>(P, tiles, nT, tu, lim, sc, faces, dq, fluxBuf, q0);   \
+        batchFluxXformKernel<DD, true><<<nT, 256, 0, st>>>(P, tiles, nT, tu, stage, faces, fluxBuf, q1);             \
+    } else {                                                                                                        \
+        batchFluxCorrKernel<DD, LIM, false><<<persistentBlocks(batchFluxCorrKernel<DD, LIM, false>, 0,               \
+                                                               tu.blocksPerSM, nT), 256, 0, st>>>(                  \
+            P, tiles, nT, tu, lim, sc, faces, dq, fluxBuf, q0);                                                     \
+        batchFluxXformKernel<DD, false><<<persistentBlocks(batchFluxXformKernel<DD, false>, 0, tu.blocksPerSM, nT),  \
+                                          256, 0, st>>>(P, tiles, nT, tu, stage, faces, fluxBuf, q1);               \
+    }
     if (dim == 1) { L(1); }
     else if (dim == 2) { L(2); }
     else { L(3); }
