@@ -66,6 +66,7 @@ SIGNATURES = {
     "hgpu_checkpoint_backward": (ctypes.c_int, [_P, _P, _P]),
     "hgpu_checkpoint_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "hgpu_checkpoint_destroy": (ctypes.c_int, [_P]),
+    "hgpu_limiter_selftest": (ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
     "hgpu_fp64_selftest": (ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_longlong)]),
     "hgpu_display": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t]),
@@ -116,6 +117,13 @@ def fp64_selftest(cases=1 << 26, seed=1):
     m, d = ctypes.c_longlong(), ctypes.c_longlong()
     check(lib().hgpu_fp64_selftest(int(seed), int(cases), ctypes.byref(m), ctypes.byref(d)))
     return m.value, d.value
+
+
+def limiter_selftest(cases=1 << 26, seed=1):
+    """Mismatches of the bit-pattern MinMod/Superbee against their fmin/fmax expressions."""
+    m = ctypes.c_longlong()
+    check(lib().hgpu_limiter_selftest(int(seed), int(cases), ctypes.byref(m)))
+    return m.value
 
 
 def fp64_peak():

@@ -14,6 +14,7 @@
 namespace hgpu {
 double measureFp64FmaRate();
 int selftestFp64Ops(unsigned long long seed, long long cases, long long* mulBad, long long* divBad);
+int selftestLimiters(unsigned long long seed, long long cases, long long* bad);
 void setLastError(const std::string& msg);
 }
 
@@ -702,6 +703,15 @@ int hgpu_fp64_selftest(unsigned long long seed, long long cases, long long* mul_
     return guarded([&]() {
         if (hgpu::selftestFp64Ops(seed, cases, mul_mismatches, div_mismatches) != 0)
             throw hgpu::CudaError(cudaGetLastError(), "fp64 self-test");
+        return (int)HGPU_OK;
+    });
+}
+
+int hgpu_limiter_selftest(unsigned long long seed, long long cases, long long* mismatches) {
+    if (!mismatches || cases < 0) return fail(HGPU_ERR_ARG, "bad argument");
+    return guarded([&]() {
+        if (hgpu::selftestLimiters(seed, cases, mismatches) != 0)
+            throw hgpu::CudaError(cudaGetLastError(), "limiter self-test");
         return (int)HGPU_OK;
     });
 }

@@ -129,10 +129,31 @@ __device__ __forceinline__ double minmodBits(double r) {
 }
 __device__ __forceinline__ float minmodBits(float r) { return fmaxLibm(0.f, fminLibm(r, 1.f)); }
 
+// Superbee, max(0, max(min(1, 2r), min(2, r))) with the same semantics, decided on the
+// bit pattern: NaN and r >= 2 give 2, (1, 2) gives r, [1/2, 1] gives 1, (+0, 1/2) gives
+// 2r (exact: the exponent field + 1, or the pattern doubled for a subnormal r), +0
+// gives +0, -0 gives -0 (every fmin/fmax of the chain then takes its second, equal
+// operand), any other negative gives +0.
+__device__ __forceinline__ double superbeeBits(double r) {
+    const long long b = bitsOf(r);
+    const long long half = 0x3FE0000000000000LL, one = 0x3FF0000000000000LL, two = 0x4000000000000000LL;
+    long long out;
+    if (isNaNBits(r) || b >= two) out = two;
+    else if (b >= one) out = b;
+    else if (b >= half) out = one;
+    else if (b > 0) out = b < (1LL << 52) ? b << 1 : b + (1LL << 52);
+    else out = b == (long long)0x8000000000000000ULL ? b : 0LL;
+    return fromBits(out);
+}
+__device__ __forceinline__ float superbeeBits(float r) {
+    return fmaxLibm(0.f, fmaxLibm(fminLibm(1.f, 2.f * r), fminLibm(2.f, r)));
+}
+
 template <typename real>
 __device__ __forceinline__ real slopeLimiter(int lim, real r) {
     typedef double W;
     if (lim == 8) return minmodBits(r);                                                         // MinMod
+    if (lim == 18) return superbeeBits(r);                                                      // Superbee
 #define MN fminLibm
 #define MX fmaxLibm
     switch (lim) {

@@ -1,10 +1,11 @@
 // probe.cu -- FP64 fused multiply-add issue-rate probe (the FP64 roofline denominator),
-// and a self-test of the integer-pipe product and quotient (fp64ops.cuh) against the
-// FP64 unit.  Eight independent dependency chains per thread keep the FP64 pipe busy;
+// a self-test of the integer-pipe product and quotient (fp64ops.cuh) against the
+// FP64 unit, and one of the bit-pattern MinMod and Superbee (common.cuh) against their
+// fmin/fmax expressions.  Eight independent dependency chains per thread keep the FP64 pipe busy;
 // every thread writes one result, so nothing is optimised away and every store is in bounds.
 #include <cuda_runtime.h>
 
-#include "fp64ops.cuh"
+#include "common.cuh"
 
 namespace hgpu {
 namespace {
@@ -53,7 +54,42 @@ __global__ void selftestKernel(unsigned long long seed, long long cases, unsigne
     if (nm) atomicAdd(&bad[0], nm);
     if (nd) atomicAdd(&bad[1], nd);
 }
+// the limiters' res/SlopeLimiter.cl expressions with C-library fmin/fmax semantics
+__device__ double minmodExpr(double r) { return fmaxLibm(0., fminLibm(r, 1.)); }
+__device__ double superbeeExpr(double r) { return fmaxLibm(0., fmaxLibm(fminLibm(1., 2. * r), fminLibm(2., r))); }
+
+// r: a seeded operand of any class, or a quotient of two (the ratios the flux forms)
+__global__ void limiterSelftestKernel(unsigned long long seed, long long cases, unsigned long long* bad) {
+    unsigned long long n = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cases;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long s = splitmix(seed + (unsigned long long)i);
+        double r = operand(s, (int)(s % 5));
+        if ((s >> 40) & 1) r = r / operand(s ^ 0x1234567ull, (int)((s >> 8) % 5));
+        if (bitsOf(minmodBits(r)) != bitsOf(minmodExpr(r))) ++n;
+        if (bitsOf(superbeeBits(r)) != bitsOf(superbeeExpr(r))) ++n;
+    }
+    if (n) atomicAdd(bad, n);
+}
 }  // namespace
+
+// mismatches (bit patterns, signs of zero included) of the bit-pattern MinMod and
+// Superbee against their expressions over `cases` seeded ratios
+int selftestLimiters(unsigned long long seed, long long cases, long long* bad) {
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return -1;
+    cudaMemset(d, 0, sizeof(unsigned long long));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    limiterSelftestKernel<<<sms * 8, 256>>>(seed, cases, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *bad = (long long)h;
+    return 0;
+}
 
 // mismatches of mulI / divI against the FP64 unit over `cases` seeded operand pairs
 int selftestFp64Ops(unsigned long long seed, long long cases, long long* mulBad, long long* divBad) {

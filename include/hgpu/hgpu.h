@@ -446,6 +446,10 @@ int hgpu_fp64_peak(double* fma_per_second);
  * of differing results (NaN == NaN). */
 int hgpu_fp64_selftest(unsigned long long seed, long long cases, long long* mul_mismatches,
                        long long* div_mismatches);
+/* Self-test of the kernels' bit-pattern MinMod and Superbee (FP64): compares them with
+ * the res/SlopeLimiter.cl expressions under C-library fmin/fmax semantics, bit for bit
+ * (signs of zero included), on `cases` seeded ratios; returns the mismatch count. */
+int hgpu_limiter_selftest(unsigned long long seed, long long cases, long long* mismatches);
 
 #ifdef __cplusplus
 }
