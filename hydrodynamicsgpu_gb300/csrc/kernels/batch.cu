@@ -77,22 +77,23 @@ __global__ void __launch_bounds__(256) batchRoeBasisKernel(const BatchProblem<re
     }
 }
 
-template <typename real, int D>
+template <typename real, int D, bool PLAIN>
 __global__ void __launch_bounds__(256) batchDtKernel(const BatchProblem<real>* __restrict__ P,
                                                      const BatchTile* __restrict__ tiles, int nT, BatchTuning tu, int hllc,
                                                      const real* __restrict__ faces, unsigned long long* acc,
                                                      unsigned* health, unsigned* q) {
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
+        const Grid g = pr.g;
         int x, y, z;
         long long c;
         unsigned long long best = ~0ULL;
         bool nan = false;
-        for (int r = 0; r < tu.cpt; ++r)
-            if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) {
-                unsigned long long b = hllc ? hllcDtCell<real, D>(pr.g, pr.ph, faces + pr.faceOff, c, x, y, z, nan)
-                                            : roeDtCell<real, D>(pr.g, pr.ph, faces + pr.faceOff, c, x, y, z, nan);
+        for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r)
+            if (tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) {
+                unsigned long long b = hllc ? hllcDtCell<real, D>(g, pr.ph, faces + pr.faceOff, c, x, y, z, nan)
+                                            : roeDtCell<real, D>(g, pr.ph, faces + pr.faceOff, c, x, y, z, nan);
                 best = b < best ? b : best;
             }
         if (nan) atomicOr(health, HEALTH_NONFINITE_DT);
@@ -171,20 +172,21 @@ __global__ void __launch_bounds__(256) batchGravityKernel(const BatchProblem<rea
 }
 
 // the state check (health.cuh) of every problem: bits into the problem's word and the batch's
-template <typename real, int D>
+template <typename real, int D, bool PLAIN>
 __global__ void __launch_bounds__(256) batchStateCheckKernel(const BatchProblem<real>* __restrict__ P,
                                                              const BatchTile* __restrict__ tiles, int nT,
                                                              BatchTuning tu, const real* __restrict__ state,
                                                              unsigned* health, unsigned* healthP, unsigned* q) {
-    for (int t = firstItem(q, tu); t < nT; t = nextItemAfter(q, tu)) {
+    for (int t = firstTile<PLAIN>(q); t < nT; t = nextTile<PLAIN>(q, nT)) {
         const BatchTile tl = tiles[t];
         const BatchProblem<real>& pr = P[tl.p];
+        const Grid g = pr.g;
         int x, y, z;
         long long c;
         unsigned bits = 0;
-        for (int r = 0; r < tu.cpt; ++r)
-        if (tileCell(pr.g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
-            bits |= stateCheckCell<real, D>(pr.g, state + (long long)(D + 2) * pr.stateOff, nullptr, c, x, y, z);
+        for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r)
+        if (tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
+            bits |= stateCheckCell<real, D>(g, state + (long long)(D + 2) * pr.stateOff, nullptr, c, x, y, z);
         warpHealthOr(bits, healthP + tl.p, health);
     }
 }
@@ -257,10 +259,15 @@ void BatchLaunch<real>::waves(int hll, unsigned* q) const {
 
 template <typename real>
 void BatchLaunch<real>::dt(int hllc, unsigned long long* acc, unsigned* health, unsigned* q) const {
-#define L(DD) batchDtKernel<real, DD><<<persistentBlocks(batchDtKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, hllc, faces, acc, health, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
+#define L(DD)                                                                                                      \
+    if (tu.blocksPerSM < 0 && tu.cpt == 1)                                                                         \
+        batchDtKernel<real, DD, true><<<nT, 256, 0, st>>>(P, tiles, nT, tu, hllc, faces, acc, health, q);           \
+    else                                                                                                           \
+        batchDtKernel<real, DD, false><<<persistentBlocks(batchDtKernel<real, DD, false>, 0, tu.blocksPerSM, nT),   \
+                                         256, 0, st>>>(P, tiles, nT, tu, hllc, faces, acc, health, q)
+    if (dim == 1) { L(1); }
+    else if (dim == 2) { L(2); }
+    else { L(3); }
 #undef L
 }
 
@@ -311,10 +318,16 @@ void BatchLaunch<real>::gravity(int integ, const StepConst<real>* sc, unsigned* 
 
 template <typename real>
 void BatchLaunch<real>::stateCheck(unsigned* health, unsigned* healthP, unsigned* q) const {
-#define L(DD) batchStateCheckKernel<real, DD><<<persistentBlocks(batchStateCheckKernel<real, DD>, 0, tu.blocksPerSM, nT), 256, 0, st>>>(P, tiles, nT, tu, state, health, healthP, q)
-    if (dim == 1) L(1);
-    else if (dim == 2) L(2);
-    else L(3);
+#define L(DD)                                                                                                      \
+    if (tu.blocksPerSM < 0 && tu.cpt == 1)                                                                         \
+        batchStateCheckKernel<real, DD, true><<<nT, 256, 0, st>>>(P, tiles, nT, tu, state, health, healthP, q);     \
+    else                                                                                                           \
+        batchStateCheckKernel<real, DD, false><<<persistentBlocks(batchStateCheckKernel<real, DD, false>, 0,        \
+                                                                  tu.blocksPerSM, nT), 256, 0, st>>>(               \
+            P, tiles, nT, tu, state, health, healthP, q)
+    if (dim == 1) { L(1); }
+    else if (dim == 2) { L(2); }
+    else { L(3); }
 #undef L
 }
 

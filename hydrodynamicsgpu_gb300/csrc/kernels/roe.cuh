@@ -17,6 +17,16 @@
 
 namespace hgpu {
 
+// A product on the FP64 unit, never contracted into an fma (so the same in translation
+// units built with and without --fmad=false).  The eigenbasis kernel issues far more
+// integer than FP64 instructions (its quotients and the record's products on the
+// integer pipes, the FP64 unit at ~59 %): its per-cell products and the left rows'
+// products run here instead of through mulI, which balanced the pipes (KH 2048^2 step
+// 7.703 -> 7.688 ms, the 512-problem batched sweep 24.42 -> 24.17 ms; every product
+// through mulN was slower, 7.82 ms).
+__device__ __forceinline__ double mulN(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mulN(float a, float b) { return __fmul_rn(a, b); }
+
 // record layout (per face, normal frame)
 template <int D>
 struct RoeRec {
@@ -65,16 +75,16 @@ __device__ __forceinline__ void roePrim(const real* s, real gamma, RoePrim<real,
 #pragma unroll
     for (int k = 0; k < D; ++k) P.v[k] = divByRecip(s[1 + k], rho, invDensity);
     // dot(v,v) over 4 components; the zero components add +0 to a non-negative sum
-    real vv = mulI(P.v[0], P.v[0]);
+    real vv = mulN(P.v[0], P.v[0]);
 #pragma unroll
-    for (int k = 1; k < D; ++k) vv = vv + mulI(P.v[k], P.v[k]);
-    real energyTotal = mulI(s[E], invDensity);
+    for (int k = 1; k < D; ++k) vv = vv + mulN(P.v[k], P.v[k]);
+    real energyTotal = mulN(s[E], invDensity);
     real energyKinetic = halfOf(vv);                                     // .5f * dot(v, v)
     real energyInternal = energyTotal - energyKinetic;                   // - energyPotential
     if (GRAV) energyInternal = energyInternal - phi;
     P.phi = phi;
-    real pressure = mulI(mulI(gm1, rho), energyInternal);
-    P.h = energyTotal + mulI(pressure, invDensity);
+    real pressure = mulN(mulN(gm1, rho), energyInternal);
+    P.h = energyTotal + mulN(pressure, invDensity);
     P.w = sqrt(rho);
 }
 
@@ -114,20 +124,20 @@ __device__ __forceinline__ void roeBasisFromPrim(const RoePrim<real, D>& L, cons
     for (int t = 0; t < D - 1; ++t) rec[R_::VT + t] = vt[t];
     rec[R_::HP] = enthalpyTotal + cvx;
     real invDenom = divI((real).5f, mulI(c, c));
-    real hv = mulI(mulI((real).5f, gm1), velocitySq);                    // .5f * (gamma - 1.f) * velocitySq
-    real gvx = mulI(gm1, vx);
-    rec[R_::L0 + 0] = mulI(hv + cvx, invDenom);
-    rec[R_::L0 + 1] = mulI(-(c + gvx), invDenom);
+    real hv = mulN(mulN((real).5f, gm1), velocitySq);                    // .5f * (gamma - 1.f) * velocitySq
+    real gvx = mulN(gm1, vx);
+    rec[R_::L0 + 0] = mulN(hv + cvx, invDenom);
+    rec[R_::L0 + 1] = mulN(-(c + gvx), invDenom);
 #pragma unroll
-    for (int t = 0; t < D - 1; ++t) rec[R_::L0 + 2 + t] = mulI(mulI(-gm1, vt[t]), invDenom);
-    rec[R_::L0 + E] = mulI(gm1, invDenom);
-    rec[R_::L1 + 0] = (real)1.f - mulI(mulI(gm1, velocitySq), invDenom);
-    rec[R_::L1 + 1] = mulI(mulI(gvx, (real)2.f), invDenom);
+    for (int t = 0; t < D - 1; ++t) rec[R_::L0 + 2 + t] = mulN(mulN(-gm1, vt[t]), invDenom);
+    rec[R_::L0 + E] = mulN(gm1, invDenom);
+    rec[R_::L1 + 0] = (real)1.f - mulN(mulN(gm1, velocitySq), invDenom);
+    rec[R_::L1 + 1] = mulN(mulN(gvx, (real)2.f), invDenom);
 #pragma unroll
-    for (int t = 0; t < D - 1; ++t) rec[R_::L1 + 2 + t] = mulI(mulI(mulI(gm1, vt[t]), (real)2.f), invDenom);
-    rec[R_::L1 + E] = mulI(mulI(-gm1, (real)2.f), invDenom);
-    rec[R_::LE0] = mulI(hv - cvx, invDenom);
-    rec[R_::LE1] = mulI(c - gvx, invDenom);
+    for (int t = 0; t < D - 1; ++t) rec[R_::L1 + 2 + t] = mulN(mulN(mulN(gm1, vt[t]), (real)2.f), invDenom);
+    rec[R_::L1 + E] = mulN(mulN(-gm1, (real)2.f), invDenom);
+    rec[R_::LE0] = mulN(hv - cvx, invDenom);
+    rec[R_::LE1] = mulN(c - gvx, invDenom);
 }
 
 // Eigen basis of one interface from the two cell states.
