@@ -389,11 +389,11 @@ void RungeKutta<real>::integrate(const std::function<void(real* stage)>& compute
     Solver<real>* s = this->solver;
     for (int k = 0; k < order_; ++k) {
         real* in = plans_[k].slot[inputSlot_[k]];
-        computeFlux(in);
-        if (k == order_ - 1 && this->lastCombine) {
-            this->lastCombine(plans_[k]);
+        if (k == order_ - 1 && this->lastStage) {
+            this->lastStage(in, plans_[k]);
             continue;
         }
+        computeFlux(in);
         s->launch("flux_divergence_combine", 1, [&] {
             launchDerivCombine<real>(s->rc.grid, s->ph, s->flux.template as<real>(), plans_[k], s->sc(), s->stream);
         });
@@ -453,6 +453,8 @@ Solver<real>::~Solver() {
     integrator.reset();
     for (cudaEvent_t e : pipeEvents_) cudaEventDestroy(e);
     if (copyStream_) cudaStreamDestroy(copyStream_);
+    if (prepStream_) cudaStreamDestroy(prepStream_);
+    if (sideStream_) cudaStreamDestroy(sideStream_);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -603,17 +605,21 @@ bool Solver<real>::hostPipelined() const {
 // The slowest axis (y in 2D, z in 3D) is cut into bands of slow-axis tiles.  Upload:
 // band after band goes up on the copy stream, the last band first (it holds the planes
 // the periodic / mirror / free-flow fill of the first ghost planes reads), then band
-// 0, 1, ...; the solver's stream takes each band as it lands: E += 0 (the zero
-// potential's resetState pass), the ghost fill of the other axes on the band's planes,
-// then the band's share of the eigenbasis (or wave speeds), which reads the band's
-// planes and the one below.  The slow axis's own ghost fill runs once the first and
-// last bands are in, before the first band's share.  Download: the last stage's combine runs band
-// by band and each band goes down as soon as it is written.  Every cell sees the same
-// operations as in set_state + update + get_state, so the results are the same bits.
+// 0, 1, ...; a preparation stream takes each band as it lands: E += 0 (the zero
+// potential's resetState pass) and the ghost fill of the other axes on the band's
+// planes; the slow axis's own ghost fill runs once the first and last bands are in.
+// Each band's share of the eigenbasis (or wave speeds), which reads the band's planes
+// and the one below, follows its preparation on one of two streams (alternate bands),
+// so consecutive bands overlap.  Download: the last stage runs band by band, its
+// fluxes on the solver's stream and each band's combine on the side stream as soon as
+// the fluxes it reads are there, and each band goes down as soon as it is written.
+// Every cell sees the same operations as in set_state + update + get_state, so the
+// results are the same bits.
 template <typename real>
 void Solver<real>::hostStep(const void* in, void* out, bool upload, bool download) {
     this->launches_ = 0;
-    if (!copyStream_) cudaCheck(cudaStreamCreateWithFlags(&copyStream_, cudaStreamNonBlocking), "copy stream");
+    for (cudaStream_t* sp : {&copyStream_, &prepStream_, &sideStream_})
+        if (!*sp) cudaCheck(cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking), "update_host stream");
     const Grid& g = rc.grid;
     const int A = rc.dim - 1;                                       // slowest axis
     const long long S_A = g.S[A];
@@ -652,31 +658,57 @@ void Solver<real>::hostStep(const void* in, void* out, bool upload, bool downloa
             landed[j] = pipeEvent(ev++);
             cudaCheck(cudaEventRecord(landed[j], copyStream_), "event record");
         }
+        // the preparation of each band as it lands, on its own stream (after the zeroing
+        // of the potential); prepped[j]: band j is ready, and so is every band prepared
+        // before it (prep order K-1, 0, then the slow axis's fill, then 1 .. K-2)
+        cudaEvent_t zeroed = pipeEvent(ev++);
+        cudaCheck(cudaEventRecord(zeroed, stream), "event record");
+        cudaCheck(cudaStreamWaitEvent(prepStream_, zeroed, 0), "stream wait");
+        std::vector<cudaEvent_t> prepped(K);
         auto prep = [&](int j) {
-            cudaCheck(cudaStreamWaitEvent(stream, landed[j], 0), "stream wait");
+            cudaCheck(cudaStreamWaitEvent(prepStream_, landed[j], 0), "stream wait");
             launch("potential_init", 1, [&] {
-                launchPotentialInit<real>(g, 0, state.as<real>(), potential.as<real>(), stream, plane0(j) * plane,
-                                          plane1(j) * plane);
+                launchPotentialInit<real>(g, 0, state.as<real>(), potential.as<real>(), prepStream_,
+                                          plane0(j) * plane, plane1(j) * plane);
             });
             for (int a = 0; a < A; ++a) {
                 // lines of axis a through the band: t = c[T] + S[T] c[U] with U the slow axis
                 // in 3D (S[T] lines a plane), T the slow axis in 2D (one line a plane)
                 const long long perPlane = rc.dim == 2 ? 1 : g.S[a == 0 ? 1 : 0];
                 launch("boundary", 1, [&] {
-                    launchBoundaryAxis<real>(g, methods, state.as<real>(), stream, a, plane0(j) * perPlane,
+                    launchBoundaryAxis<real>(g, methods, state.as<real>(), prepStream_, a, plane0(j) * perPlane,
                                              plane1(j) * perPlane);
                 });
             }
         };
+        auto mark = [&](int j) {
+            prepped[j] = pipeEvent(ev++);
+            cudaCheck(cudaEventRecord(prepped[j], prepStream_), "event record");
+        };
         prep(K - 1);
         if (K > 1) prep(0);
-        launch("boundary", 1, [&] { launchBoundaryAxis<real>(g, methods, state.as<real>(), stream, A); });
-        bandedPrologueWork((int)tile0(0), (int)(tile1(0) - tile0(0)));
+        launch("boundary", 1, [&] { launchBoundaryAxis<real>(g, methods, state.as<real>(), prepStream_, A); });
+        mark(0);
+        if (K > 1) prepped[K - 1] = prepped[0];
         for (int j = 1; j < K - 1; ++j) {
             prep(j);
-            bandedPrologueWork((int)tile0(j), (int)(tile1(j) - tile0(j)));
+            mark(j);
         }
-        if (K > 1) bandedPrologueWork((int)tile0(K - 1), (int)(tile1(K - 1) - tile0(K - 1)));
+        // each band's eigenbasis (wave speeds) once its planes and the plane below are
+        // ready, bands alternating between two streams: a band's kernel reads no other
+        // band's output, so consecutive bands overlap (and fill each other's tail wave)
+        cudaEvent_t sideLast = nullptr;
+        for (int j = 0; j < K; ++j) {
+            cudaStream_t bs = (j & 1) ? sideStream_ : stream;
+            const int need = (j == K - 1 && K > 2) ? K - 2 : j;     // band K-1 reads band K-2's top plane
+            cudaCheck(cudaStreamWaitEvent(bs, prepped[need], 0), "stream wait");
+            bandedPrologueWork((int)tile0(j), (int)(tile1(j) - tile0(j)), bs);
+            if (bs == sideStream_) {
+                sideLast = pipeEvent(ev++);
+                cudaCheck(cudaEventRecord(sideLast, sideStream_), "event record");
+            }
+        }
+        if (sideLast) cudaCheck(cudaStreamWaitEvent(stream, sideLast, 0), "stream wait");
         bandedPrologueEnd();
     } else {
         boundary();
@@ -685,26 +717,42 @@ void Solver<real>::hostStep(const void* in, void* out, bool upload, bool downloa
     }
     finalizeDt(false);
 
-    const bool banded = download && integrator->lastCombineWritesState() && !fusedActive();
+    const bool banded = download && integrator->lastCombineWritesState() && !fusedActive() && fluxByPlanes();
     struct Unhook {
         Integrator<real>* i;
-        ~Unhook() { i->lastCombine = nullptr; }
+        ~Unhook() { i->lastStage = nullptr; }
     } unhook{integrator.get()};
     if (banded) {
-        integrator->lastCombine = [&](const CombinePlan<real>& plan) {
+        // The last stage band by band: on the solver's stream the fluxes the band's
+        // combine reads (planes [p0, p1], continuing from the previous band's); on the
+        // side stream the band's combine once they are there, then its download.  The
+        // fluxes of band j+1 overlap the combine of band j: they write flux planes past
+        // p1(j) and read the stage input, which the last combine (it writes the state,
+        // never its own stage's input) does not touch.
+        integrator->lastStage = [&](real* stageIn, const CombinePlan<real>& plan) {
+            long long fluxDone = 0, dqDone = 0;
             for (int j = 0; j < K; ++j) {
+                const long long fEnd = std::min<long long>(plane1(j) + 1, S_A);
+                fluxPlanes(stageIn, fluxDone, fEnd, dqDone);
+                fluxDone = fEnd;
+                cudaEvent_t fluxed = pipeEvent(ev++);
+                cudaCheck(cudaEventRecord(fluxed, stream), "event record");
+                cudaCheck(cudaStreamWaitEvent(sideStream_, fluxed, 0), "stream wait");
                 launch("flux_divergence_combine", 1, [&] {
-                    launchDerivCombine<real>(g, ph, flux.template as<real>(), plan, sc(), stream, plane0(j) * plane,
-                                             plane1(j) * plane);
+                    launchDerivCombine<real>(g, ph, flux.template as<real>(), plan, sc(), sideStream_,
+                                             plane0(j) * plane, plane1(j) * plane);
                 });
                 cudaEvent_t written = pipeEvent(ev++);
-                cudaCheck(cudaEventRecord(written, stream), "event record");
+                cudaCheck(cudaEventRecord(written, sideStream_), "event record");
                 cudaCheck(cudaStreamWaitEvent(copyStream_, written, 0), "stream wait");
                 cudaCheck(cudaMemcpyAsync(static_cast<char*>(out) + offOf(plane0(j)),
                                           static_cast<const char*>(state.get()) + offOf(plane0(j)),
                                           bytesOf(plane1(j) - plane0(j)), cudaMemcpyDeviceToHost, copyStream_),
                           "update_host download");
             }
+            cudaEvent_t combined = pipeEvent(ev++);
+            cudaCheck(cudaEventRecord(combined, sideStream_), "event record");
+            cudaCheck(cudaStreamWaitEvent(stream, combined, 0), "stream wait");
         };
     }
     step();
@@ -797,10 +845,10 @@ void Roe<real>::calcTimestep() {                             // Roe::calcTimeste
 // the eigenbasis of the faces of the band's cells (it reads the band's planes and the
 // plane below the band)
 template <typename real>
-void Roe<real>::bandedPrologueWork(int tile0, int tiles) {
+void Roe<real>::bandedPrologueWork(int tile0, int tiles, cudaStream_t st) {
     this->launch("roe_eigenbasis", 1, [&] {
         launchRoeBasis<real>(this->rc.grid, this->ph, this->state.template as<real>(), basis.template as<real>(),
-                             this->rc.cfg.compat == HGPU_COMPAT_SEAM, this->stream, nullptr, tile0, tiles);
+                             this->rc.cfg.compat == HGPU_COMPAT_SEAM, st, nullptr, tile0, tiles);
     });
 }
 
@@ -817,6 +865,30 @@ void Roe<real>::calcFlux(real* stage) {                      // Roe::calcDeriv (
         launchRoeFlux<real>(this->rc.grid, this->rc.cfg.limiter, stage, basis.template as<real>(),
                             deltaQTilde.template as<real>(), this->sc(), this->flux.template as<real>(), seam,
                             this->stream);
+    });
+}
+
+// calcFlux on the faces of slow-axis planes [from, to): the flux of plane q reads the
+// Delta-q-tilde of planes q-1, q, q+1, which reads the stage's planes q-1 .. q+1 and
+// the eigenbasis of its own plane
+template <typename real>
+void Roe<real>::fluxPlanes(real* stage, long long from, long long to, long long& dqDone) {
+    const Grid& g = this->rc.grid;
+    const long long S = g.S[this->rc.dim - 1], plane = (long long)g.V / S;
+    const bool seam = this->rc.cfg.compat == HGPU_COMPAT_SEAM;
+    if (from == 0 && dqDone == 0 && seam && stage != this->state.template as<real>()) this->boundaryOn(stage);
+    const long long dqEnd = std::min(to + 1, S);
+    if (dqEnd > dqDone) {
+        this->launch("roe_delta_q_tilde", 1, [&] {
+            launchRoeDeltaQ<real>(g, stage, basis.template as<real>(), deltaQTilde.template as<real>(), seam,
+                                  this->stream, dqDone * plane, dqEnd * plane);
+        });
+        dqDone = dqEnd;
+    }
+    if (to <= from) return;
+    this->launch("roe_flux", sizeof(real) == 8 ? 2 : 1, [&] {
+        launchRoeFlux<real>(g, this->rc.cfg.limiter, stage, basis.template as<real>(), deltaQTilde.template as<real>(),
+                            this->sc(), this->flux.template as<real>(), seam, this->stream, from * plane, to * plane);
     });
 }
 
@@ -897,14 +969,14 @@ void HLL<real>::initStep() {                                 // HLL::initStep (H
 // the wave speeds of the faces of the band's cells (they read the band's planes and
 // the plane below the band)
 template <typename real>
-void HLL<real>::bandedPrologueWork(int tile0, int tiles) {
+void HLL<real>::bandedPrologueWork(int tile0, int tiles, cudaStream_t st) {
     const Grid& g = this->rc.grid;
     const int T_A = this->slowTile();
     const long long S_A = g.S[this->rc.dim - 1], plane = (long long)g.V / S_A;
     const long long p0 = (long long)tile0 * T_A, p1 = std::min<long long>((long long)(tile0 + tiles) * T_A, S_A);
     this->launch("hllc_wave_speeds", 1, [&] {
         launchHllcWaves<real>(g, this->ph, this->state.template as<real>(), waves.template as<real>(),
-                              this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream, nullptr, p0 * plane, p1 * plane);
+                              this->rc.cfg.solver == HGPU_SOLVER_HLL, st, nullptr, p0 * plane, p1 * plane);
     });
 }
 
@@ -926,6 +998,23 @@ void HLL<real>::step() {                                     // HLL::step (HLL.c
                                  this->flux.template as<real>(), this->health, this->rc.cfg.solver == HGPU_SOLVER_HLL,
                                  this->stream, this->livePotential());
         });
+    });
+}
+
+// the flux of faces of slow-axis planes [from, to) (each reads the stage's planes q-1, q
+// and the wave speeds of plane q)
+template <typename real>
+void HLL<real>::fluxPlanes(real* stage, long long from, long long to, long long& dqDone) {
+    (void)dqDone;
+    const Grid& g = this->rc.grid;
+    const long long plane = (long long)g.V / g.S[this->rc.dim - 1];
+    if (from == 0 && this->rc.cfg.compat == HGPU_COMPAT_SEAM && stage != this->state.template as<real>())
+        this->boundaryOn(stage);
+    if (to <= from) return;
+    this->launch("hllc_flux", 1, [&] {
+        launchHllcFlux<real>(g, this->ph, stage, waves.template as<real>(), this->flux.template as<real>(),
+                             this->health, this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream,
+                             this->livePotential(), from * plane, to * plane);
     });
 }
 

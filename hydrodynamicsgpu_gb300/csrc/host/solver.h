@@ -129,8 +129,9 @@ public:
     // true when the last stage's combine writes the new state and nothing after it in
     // the step (the self-gravity pass with a zero potential) touches the state again
     virtual bool lastCombineWritesState() const { return false; }
-    // when set, the last stage's combine is handed to this instead of launched whole
-    std::function<void(const CombinePlan<real>&)> lastCombine;
+    // when set, the last stage (its fluxes and its combine) is handed to this instead
+    // of launched whole
+    std::function<void(real* stage, const CombinePlan<real>&)> lastStage;
 protected:
     Solver<real>* solver;
 };
@@ -285,13 +286,23 @@ protected:
     // band is done (bandedPrologueEnd).
     virtual bool bandedPrologue() const { return false; }
     virtual int slowTile() const { return 1; }
-    virtual void bandedPrologueWork(int tile0, int tiles) { (void)tile0; (void)tiles; }
+    virtual void bandedPrologueWork(int tile0, int tiles, cudaStream_t st) { (void)tile0; (void)tiles; (void)st; }
     virtual void bandedPrologueEnd() {}
     // the stages run as fused kernels (no separate combine to cut in bands)
     virtual bool fusedActive() const { return false; }
+    // The interface fluxes of `stage` on the faces of slow-axis planes [from, to), the
+    // same values calcFlux leaves for the whole grid; called for consecutive ranges from
+    // plane 0 (EulerRoe also forms the Delta-q-tilde planes they read, continuing from
+    // dqDone).  hostStep runs the last stage this way, band by band.
+    virtual bool fluxByPlanes() const { return false; }
+    virtual void fluxPlanes(real* stage, long long from, long long to, long long& dqDone) {
+        (void)stage; (void)from; (void)to; (void)dqDone;
+    }
 
 private:
     cudaStream_t copyStream_ = nullptr;     // update_host's uploads and downloads
+    cudaStream_t prepStream_ = nullptr;     // update_host: the bands' preparation as they land
+    cudaStream_t sideStream_ = nullptr;     // update_host: every other band's eigenbasis, the last combines
     std::vector<cudaEvent_t> pipeEvents_;
     cudaEvent_t pipeEvent(size_t i);
 };
@@ -324,8 +335,10 @@ protected:
     void calcFlux(real* stage);                   // calcDeltaQTilde + calcFlux
     bool bandedPrologue() const override { return !this->livePotential(); }
     int slowTile() const override { return roeBasisSlowTile(this->rc.dim); }
-    void bandedPrologueWork(int tile0, int tiles) override;
+    void bandedPrologueWork(int tile0, int tiles, cudaStream_t st) override;
     void bandedPrologueEnd() override { cflReduce(); }
+    bool fluxByPlanes() const override { return true; }
+    void fluxPlanes(real* stage, long long from, long long to, long long& dqDone) override;
 public:
     int setFusedStages(bool on) override;
 };
@@ -352,8 +365,10 @@ protected:
     // bands of the wave speeds: the same plane granularity as the Roe eigenbasis bands
     bool bandedPrologue() const override { return !this->livePotential(); }
     int slowTile() const override { return roeBasisSlowTile(this->rc.dim); }
-    void bandedPrologueWork(int tile0, int tiles) override;
+    void bandedPrologueWork(int tile0, int tiles, cudaStream_t st) override;
     void bandedPrologueEnd() override { calcTimestep(); }
+    bool fluxByPlanes() const override { return true; }
+    void fluxPlanes(real* stage, long long from, long long to, long long& dqDone) override;
 };
 
 template <typename real>

@@ -49,9 +49,10 @@ __global__ void __launch_bounds__(kThreads) hllcDtKernel(Grid g, Phys<real> ph, 
 template <typename real, int D, bool HLL, bool GRAV>
 __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph, const real* __restrict__ stage,
                                                            const real* __restrict__ waves, real* __restrict__ flux,
-                                                           unsigned* health, const real* __restrict__ pot) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                           unsigned* health, const real* __restrict__ pot,
+                                                           long long c0, long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     if (!hllcFluxCell<real, D, HLL, GRAV>(g, ph, stage, waves, flux, c, x, y, z, pot))
@@ -100,9 +101,12 @@ void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsign
 
 template <typename real, bool GRAV>
 void launchHllcFluxG(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                     unsigned* health, int hll, cudaStream_t st, const real* pot) {
-#define L(DD, H) \
-    hllcFluxKernel<real, DD, H, GRAV><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, stage, waves, flux, health, pot)
+                     unsigned* health, int hll, cudaStream_t st, const real* pot, long long c0, long long c1) {
+    if (c1 < 0) c1 = g.V;
+    if (c1 <= c0) return;
+#define L(DD, H)                                                                                                  \
+    hllcFluxKernel<real, DD, H, GRAV><<<blocksFor(c1 - c0), kThreads, 0, st>>>(g, ph, stage, waves, flux, health, pot, \
+                                                                             c0, c1)
     if (hll) {
         if (g.dim == 1) L(1, true);
         else if (g.dim == 2) L(2, true);
@@ -117,9 +121,9 @@ void launchHllcFluxG(const Grid& g, const Phys<real>& ph, const real* stage, con
 
 template <typename real>
 void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                    unsigned* health, int hll, cudaStream_t st, const real* pot) {
-    if (pot) launchHllcFluxG<real, true>(g, ph, stage, waves, flux, health, hll, st, pot);
-    else launchHllcFluxG<real, false>(g, ph, stage, waves, flux, health, hll, st, nullptr);
+                    unsigned* health, int hll, cudaStream_t st, const real* pot, long long c0, long long c1) {
+    if (pot) launchHllcFluxG<real, true>(g, ph, stage, waves, flux, health, hll, st, pot, c0, c1);
+    else launchHllcFluxG<real, false>(g, ph, stage, waves, flux, health, hll, st, nullptr, c0, c1);
 }
 
 #define INST(real)                                                                                                \
@@ -128,7 +132,7 @@ void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, cons
     template void launchHllcDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                      cudaStream_t);                                                               \
     template void launchHllcFlux<real>(const Grid&, const Phys<real>&, const real*, const real*, real*, unsigned*, \
-                                       int, cudaStream_t, const real*);
+                                       int, cudaStream_t, const real*, long long, long long);
 INST(double)
 INST(float)
 #undef INST

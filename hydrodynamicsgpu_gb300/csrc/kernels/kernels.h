@@ -71,10 +71,13 @@ template <typename real>
 void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigned long long* acc, unsigned* health,
                  cudaStream_t st);
 template <typename real>
-void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* dq, int seam, cudaStream_t st);
+// cells [c0, c1) only (c1 < 0: to the end of the grid)
+void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* dq, int seam, cudaStream_t st,
+                     long long c0 = 0, long long c1 = -1);
 template <typename real>
 void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
-                   const StepConst<real>* sc, real* flux, int seam, cudaStream_t st);
+                   const StepConst<real>* sc, real* flux, int seam, cudaStream_t st, long long c0 = 0,
+                   long long c1 = -1);
 int roeRecordSize(int dim);
 
 // ---- hllc.cu ----
@@ -87,7 +90,8 @@ void launchHllcDt(const Grid& g, const Phys<real>& ph, const real* waves, unsign
                   cudaStream_t st);
 template <typename real>
 void launchHllcFlux(const Grid& g, const Phys<real>& ph, const real* stage, const real* waves, real* flux,
-                    unsigned* health, int hll, cudaStream_t st, const real* pot = nullptr);
+                    unsigned* health, int hll, cudaStream_t st, const real* pot = nullptr, long long c0 = 0,
+                    long long c1 = -1);
 
 // ---- display scalar (display.cu, convertToTex): method = the reference's DISPLAY_* index ----
 int displayCount(int dim);

@@ -62,9 +62,9 @@ __global__ void __launch_bounds__(kThreads) roeDtKernel(Grid g, Phys<real> ph, c
 template <typename real, int D>
 __global__ void __launch_bounds__(kThreads) roeDeltaQKernel(Grid g, const real* __restrict__ stage,
                                                             const real* __restrict__ basis, real* __restrict__ dq,
-                                                            int loA, int hiA) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                            int loA, int hiA, long long c0, long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     roeDeltaQCell<real, D>(g, stage, basis, dq, c, x, y, z, loA, hiA);
@@ -74,9 +74,9 @@ template <typename real, int D, int LIM>
 __global__ void __launch_bounds__(kThreads) roeFluxKernel(Grid g, int lim, const real* __restrict__ stage,
                                                           const real* __restrict__ basis, const real* __restrict__ dq,
                                                           const StepConst<real>* __restrict__ sc,
-                                                          real* __restrict__ flux) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                          real* __restrict__ flux, long long c0, long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     roeFluxCell<real, D, LIM>(g, lim, *sc, stage, basis, dq, flux, c, x, y, z);
@@ -86,9 +86,9 @@ template <int D, int LIM>
 __global__ void __launch_bounds__(kThreads) roeFluxCorrKernel(Grid g, int lim, const double* __restrict__ basis,
                                                               const double* __restrict__ dq,
                                                               const StepConst<double>* __restrict__ sc,
-                                                              double* __restrict__ flux) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                              double* __restrict__ flux, long long c0, long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     roeFluxCorrectionsCell<D, LIM>(g, lim, *sc, basis, dq, flux, c, x, y, z);
@@ -97,9 +97,9 @@ __global__ void __launch_bounds__(kThreads) roeFluxCorrKernel(Grid g, int lim, c
 template <int D>
 __global__ void __launch_bounds__(kThreads) roeFluxXformKernel(Grid g, const double* __restrict__ stage,
                                                                const double* __restrict__ basis,
-                                                               double* __restrict__ flux) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.V) return;
+                                                               double* __restrict__ flux, long long c0, long long c1) {
+    long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int x, y, z;
     cellCoords(g, c, x, y, z);
     roeFluxTransformsCell<D>(g, stage, basis, flux, c, x, y, z);
@@ -152,58 +152,71 @@ void launchRoeDt(const Grid& g, const Phys<real>& ph, const real* basis, unsigne
     else roeDtKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, ph, basis, acc, health);
 }
 
+// cells [c0, c1) (c1 < 0: to the end of the grid); whole-grid launches take every cell
+static inline long long rangeEnd(const Grid& g, long long c1) { return c1 < 0 ? g.V : c1; }
+
 template <typename real>
-void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* dq, int seam, cudaStream_t st) {
+void launchRoeDeltaQ(const Grid& g, const real* stage, const real* basis, real* dq, int seam, cudaStream_t st,
+                     long long c0, long long c1) {
     int loA = seam ? 1 : 2, hiA = seam ? 0 : 1;
-    if (g.dim == 1) roeDeltaQKernel<real, 1><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
-    else if (g.dim == 2) roeDeltaQKernel<real, 2><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
-    else roeDeltaQKernel<real, 3><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA);
+    c1 = rangeEnd(g, c1);
+    if (c1 <= c0) return;
+    const unsigned b = blocksFor(c1 - c0);
+    if (g.dim == 1) roeDeltaQKernel<real, 1><<<b, kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA, c0, c1);
+    else if (g.dim == 2) roeDeltaQKernel<real, 2><<<b, kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA, c0, c1);
+    else roeDeltaQKernel<real, 3><<<b, kThreads, 0, st>>>(g, stage, basis, dq, loA, hiA, c0, c1);
 }
 
 template <int LIM>
 void launchRoeFluxSplit(const Grid& g, int limiter, const double* stage, const double* basis, const double* dq,
-                        const StepConst<double>* sc, double* flux, cudaStream_t st) {
+                        const StepConst<double>* sc, double* flux, cudaStream_t st, long long c0, long long c1) {
+    const unsigned b = blocksFor(c1 - c0);
     if (g.dim == 1) {
-        roeFluxCorrKernel<1, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux);
-        roeFluxXformKernel<1><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, flux);
+        roeFluxCorrKernel<1, LIM><<<b, kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux, c0, c1);
+        roeFluxXformKernel<1><<<b, kThreads, 0, st>>>(g, stage, basis, flux, c0, c1);
     } else if (g.dim == 2) {
-        roeFluxCorrKernel<2, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux);
-        roeFluxXformKernel<2><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, flux);
+        roeFluxCorrKernel<2, LIM><<<b, kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux, c0, c1);
+        roeFluxXformKernel<2><<<b, kThreads, 0, st>>>(g, stage, basis, flux, c0, c1);
     } else {
-        roeFluxCorrKernel<3, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux);
-        roeFluxXformKernel<3><<<blocksFor(g.V), kThreads, 0, st>>>(g, stage, basis, flux);
+        roeFluxCorrKernel<3, LIM><<<b, kThreads, 0, st>>>(g, limiter, basis, dq, sc, flux, c0, c1);
+        roeFluxXformKernel<3><<<b, kThreads, 0, st>>>(g, stage, basis, flux, c0, c1);
     }
 }
 
 template <typename real, int LIM>
 void launchRoeFluxLim(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
-                      const StepConst<real>* sc, real* flux, cudaStream_t st) {
+                      const StepConst<real>* sc, real* flux, cudaStream_t st, long long c0, long long c1) {
     // FP64 runs the flux as two lighter passes (more resident warps, same bits)
     if (sizeof(real) == 8) {
         launchRoeFluxSplit<LIM>(g, limiter, (const double*)stage, (const double*)basis, (const double*)dq,
-                                (const StepConst<double>*)sc, (double*)flux, st);
+                                (const StepConst<double>*)sc, (double*)flux, st, c0, c1);
         return;
     }
-    if (g.dim == 1) roeFluxKernel<real, 1, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
-    else if (g.dim == 2) roeFluxKernel<real, 2, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
-    else roeFluxKernel<real, 3, LIM><<<blocksFor(g.V), kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux);
+    const unsigned b = blocksFor(c1 - c0);
+    if (g.dim == 1) roeFluxKernel<real, 1, LIM><<<b, kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux, c0, c1);
+    else if (g.dim == 2) roeFluxKernel<real, 2, LIM><<<b, kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux, c0, c1);
+    else roeFluxKernel<real, 3, LIM><<<b, kThreads, 0, st>>>(g, limiter, stage, basis, dq, sc, flux, c0, c1);
 }
 
 // the benchmark limiters and the common ones get kernels of their own; the others
 // share one kernel that dispatches on the limiter at run time
 template <typename real>
 void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* basis, const real* dq,
-                   const StepConst<real>* sc, real* flux, int seam, cudaStream_t st) {
+                   const StepConst<real>* sc, real* flux, int seam, cudaStream_t st, long long c0, long long c1) {
     (void)seam;
+    c1 = rangeEnd(g, c1);
+    if (c1 <= c0) return;
+#define F(LL) launchRoeFluxLim<real, LL>(g, limiter, stage, basis, dq, sc, flux, st, c0, c1)
     switch (limiter) {
-    case HGPU_LIMITER_DONORCELL: launchRoeFluxLim<real, HGPU_LIMITER_DONORCELL>(g, limiter, stage, basis, dq, sc, flux, st); break;
-    case HGPU_LIMITER_LAXWENDROFF: launchRoeFluxLim<real, HGPU_LIMITER_LAXWENDROFF>(g, limiter, stage, basis, dq, sc, flux, st); break;
-    case HGPU_LIMITER_MINMOD: launchRoeFluxLim<real, HGPU_LIMITER_MINMOD>(g, limiter, stage, basis, dq, sc, flux, st); break;
-    case HGPU_LIMITER_VANLEER: launchRoeFluxLim<real, HGPU_LIMITER_VANLEER>(g, limiter, stage, basis, dq, sc, flux, st); break;
-    case HGPU_LIMITER_MONOTIZEDCENTRAL: launchRoeFluxLim<real, HGPU_LIMITER_MONOTIZEDCENTRAL>(g, limiter, stage, basis, dq, sc, flux, st); break;
-    case HGPU_LIMITER_SUPERBEE: launchRoeFluxLim<real, HGPU_LIMITER_SUPERBEE>(g, limiter, stage, basis, dq, sc, flux, st); break;
-    default: launchRoeFluxLim<real, -1>(g, limiter, stage, basis, dq, sc, flux, st); break;
+    case HGPU_LIMITER_DONORCELL: F(HGPU_LIMITER_DONORCELL); break;
+    case HGPU_LIMITER_LAXWENDROFF: F(HGPU_LIMITER_LAXWENDROFF); break;
+    case HGPU_LIMITER_MINMOD: F(HGPU_LIMITER_MINMOD); break;
+    case HGPU_LIMITER_VANLEER: F(HGPU_LIMITER_VANLEER); break;
+    case HGPU_LIMITER_MONOTIZEDCENTRAL: F(HGPU_LIMITER_MONOTIZEDCENTRAL); break;
+    case HGPU_LIMITER_SUPERBEE: F(HGPU_LIMITER_SUPERBEE); break;
+    default: F(-1); break;
     }
+#undef F
 }
 
 #define INST(real)                                                                                              \
@@ -211,9 +224,10 @@ void launchRoeFlux(const Grid& g, int limiter, const real* stage, const real* ba
                                        const real*, int, int);                                                  \
     template void launchRoeDt<real>(const Grid&, const Phys<real>&, const real*, unsigned long long*, unsigned*, \
                                     cudaStream_t);                                                             \
-    template void launchRoeDeltaQ<real>(const Grid&, const real*, const real*, real*, int, cudaStream_t);       \
+    template void launchRoeDeltaQ<real>(const Grid&, const real*, const real*, real*, int, cudaStream_t,        \
+                                        long long, long long);                                                  \
     template void launchRoeFlux<real>(const Grid&, int, const real*, const real*, const real*,                   \
-                                      const StepConst<real>*, real*, int, cudaStream_t);
+                                      const StepConst<real>*, real*, int, cudaStream_t, long long, long long);
 INST(double)
 INST(float)
 #undef INST

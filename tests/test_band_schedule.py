@@ -3,13 +3,16 @@ restated and checked on the CPU for every slow-axis size 5-1099 (2D) and 5-79 (3
 
 The slowest axis (y in 2D, z in 3D) is cut into K bands of `per` eigenbasis tiles
 (T_A planes each; the last band takes the remainder).  Upload order: band K-1, then
-0, 1, ..., K-2.  On the solver's stream: prep(K-1), prep(0), the slow axis's ghost
-fill, work(0), then prep(j), work(j) for j = 1..K-2, then work(K-1).  prep(j) makes
-the band's planes ready (landed, E += 0, ghost fill of the other axes); work(j) is
-the band's eigenbasis, whose tile t reads planes t*T_A - 1 .. t*T_A + T_A - 1.
-Checked: the bands partition the axis, every plane read is ready when read, the
-slow fill's planes (2, 3, S-4, S-3 read; 0, 1, S-2, S-1 written) are all in the first
-two bands uploaded, and the other axes' line ranges stay inside their line counts."""
+0, 1, ..., K-2.  On the preparation stream, in order: prep(K-1), prep(0), the slow
+axis's ghost fill, mark(0) (band K-1 shares that mark), then prep(j), mark(j) for
+j = 1..K-2.  prep(j) makes the band's planes ready (landed, E += 0, ghost fill of the
+other axes).  work(j), the band's eigenbasis (tile t reads planes t*T_A - 1 ..
+t*T_A + T_A - 1), runs on one of two streams after mark(j) (band K-1: after
+mark(K-2)), so it may only read planes that were ready at that mark; bands' works run
+in any order relative to each other.  Checked: the bands partition the axis, every
+plane a work reads is ready at the mark it waits for, the slow fill's planes (2, 3,
+S-4, S-3 read; 0, 1, S-2, S-1 written) are all in the first two bands uploaded, and
+the other axes' line ranges stay inside their line counts."""
 import pytest
 
 
@@ -32,6 +35,7 @@ def check_schedule(dim, S):
     covered = [p for j in range(K) for p in range(p0[j], p1[j])]
     assert covered == list(range(S_A))
     ready = set()
+    marks = {}
 
     def prep(j):
         ready.update(range(p0[j], p1[j]))
@@ -41,22 +45,24 @@ def check_schedule(dim, S):
             assert 0 <= p0[j] * per_plane < p1[j] * per_plane <= lines
 
     def work(j):
+        need = K - 2 if (j == K - 1 and K > 2) else j
+        seen = marks[need]
         for t in range(t0[j], t1[j]):
             for p in range(t * T_A - 1, t * T_A + T_A):
                 if 0 <= p < S_A:
-                    assert p in ready, (dim, S, j, t, p)
+                    assert p in seen, (dim, S, j, t, p)
 
     prep(K - 1)
     if K > 1:
         prep(0)
     for p in (2, 3, S_A - 4, S_A - 3, 0, 1, S_A - 2, S_A - 1):
         assert p in ready, (dim, S, K, p)
-    work(0)
+    marks[0] = marks[K - 1] = frozenset(ready)
     for j in range(1, K - 1):
         prep(j)
+        marks[j] = frozenset(ready)
+    for j in range(K):                              # any order: each waits for its own mark
         work(j)
-    if K > 1:
-        work(K - 1)
     return K
 
 
