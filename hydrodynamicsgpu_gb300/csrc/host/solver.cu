@@ -618,8 +618,15 @@ bool Solver<real>::hostPipelined() const {
 template <typename real>
 void Solver<real>::hostStep(const void* in, void* out, bool upload, bool download) {
     this->launches_ = 0;
-    for (cudaStream_t* sp : {&copyStream_, &prepStream_, &sideStream_})
-        if (!*sp) cudaCheck(cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking), "update_host stream");
+    if (!copyStream_) {
+        int lowest = 0, highest = 0;
+        cudaCheck(cudaDeviceGetStreamPriorityRange(&lowest, &highest), "stream priorities");
+        cudaCheck(cudaStreamCreateWithFlags(&copyStream_, cudaStreamNonBlocking), "update_host stream");
+        // the bands' preparations and last combines gate the next band's work and
+        // its download: their blocks go ahead of the eigenbasis and flux blocks queued
+        cudaCheck(cudaStreamCreateWithPriority(&prepStream_, cudaStreamNonBlocking, highest), "update_host stream");
+        cudaCheck(cudaStreamCreateWithFlags(&sideStream_, cudaStreamNonBlocking), "update_host stream");
+    }
     const Grid& g = rc.grid;
     const int A = rc.dim - 1;                                       // slowest axis
     const long long S_A = g.S[A];
@@ -730,20 +737,31 @@ void Solver<real>::hostStep(const void* in, void* out, bool upload, bool downloa
         // p1(j) and read the stage input, which the last combine (it writes the state,
         // never its own stage's input) does not touch.
         integrator->lastStage = [&](real* stageIn, const CombinePlan<real>& plan) {
-            long long fluxDone = 0, dqDone = 0;
+            fluxPrepare(stageIn);
+            cudaEvent_t prepared = pipeEvent(ev++);
+            cudaCheck(cudaEventRecord(prepared, stream), "event record");
+            cudaCheck(cudaStreamWaitEvent(sideStream_, prepared, 0), "stream wait");
+            long long fluxDone = 0;
+            cudaEvent_t prevFluxed = nullptr;
             for (int j = 0; j < K; ++j) {
+                // band j's fluxes on alternating streams (they read only what fluxPrepare
+                // wrote and the stage input); its combine reads flux planes up to p1(j),
+                // written by this band's call and the previous one
+                cudaStream_t fs = (j & 1) ? sideStream_ : stream;
                 const long long fEnd = std::min<long long>(plane1(j) + 1, S_A);
-                fluxPlanes(stageIn, fluxDone, fEnd, dqDone);
+                fluxPlanes(stageIn, fluxDone, fEnd, fs);
                 fluxDone = fEnd;
                 cudaEvent_t fluxed = pipeEvent(ev++);
-                cudaCheck(cudaEventRecord(fluxed, stream), "event record");
-                cudaCheck(cudaStreamWaitEvent(sideStream_, fluxed, 0), "stream wait");
+                cudaCheck(cudaEventRecord(fluxed, fs), "event record");
+                cudaCheck(cudaStreamWaitEvent(prepStream_, fluxed, 0), "stream wait");
+                if (prevFluxed) cudaCheck(cudaStreamWaitEvent(prepStream_, prevFluxed, 0), "stream wait");
+                prevFluxed = fluxed;
                 launch("flux_divergence_combine", 1, [&] {
-                    launchDerivCombine<real>(g, ph, flux.template as<real>(), plan, sc(), sideStream_,
+                    launchDerivCombine<real>(g, ph, flux.template as<real>(), plan, sc(), prepStream_,
                                              plane0(j) * plane, plane1(j) * plane);
                 });
                 cudaEvent_t written = pipeEvent(ev++);
-                cudaCheck(cudaEventRecord(written, sideStream_), "event record");
+                cudaCheck(cudaEventRecord(written, prepStream_), "event record");
                 cudaCheck(cudaStreamWaitEvent(copyStream_, written, 0), "stream wait");
                 cudaCheck(cudaMemcpyAsync(static_cast<char*>(out) + offOf(plane0(j)),
                                           static_cast<const char*>(state.get()) + offOf(plane0(j)),
@@ -751,7 +769,7 @@ void Solver<real>::hostStep(const void* in, void* out, bool upload, bool downloa
                           "update_host download");
             }
             cudaEvent_t combined = pipeEvent(ev++);
-            cudaCheck(cudaEventRecord(combined, sideStream_), "event record");
+            cudaCheck(cudaEventRecord(combined, prepStream_), "event record");
             cudaCheck(cudaStreamWaitEvent(stream, combined, 0), "stream wait");
         };
     }
@@ -868,27 +886,27 @@ void Roe<real>::calcFlux(real* stage) {                      // Roe::calcDeriv (
     });
 }
 
-// calcFlux on the faces of slow-axis planes [from, to): the flux of plane q reads the
-// Delta-q-tilde of planes q-1, q, q+1, which reads the stage's planes q-1 .. q+1 and
-// the eigenbasis of its own plane
+// calcFlux in two parts: the ghost refresh (SEAM) and Delta-q-tilde of the whole grid,
+// then the flux of the faces of slow-axis planes [from, to) on stream st
 template <typename real>
-void Roe<real>::fluxPlanes(real* stage, long long from, long long to, long long& dqDone) {
-    const Grid& g = this->rc.grid;
-    const long long S = g.S[this->rc.dim - 1], plane = (long long)g.V / S;
+void Roe<real>::fluxPrepare(real* stage) {
     const bool seam = this->rc.cfg.compat == HGPU_COMPAT_SEAM;
-    if (from == 0 && dqDone == 0 && seam && stage != this->state.template as<real>()) this->boundaryOn(stage);
-    const long long dqEnd = std::min(to + 1, S);
-    if (dqEnd > dqDone) {
-        this->launch("roe_delta_q_tilde", 1, [&] {
-            launchRoeDeltaQ<real>(g, stage, basis.template as<real>(), deltaQTilde.template as<real>(), seam,
-                                  this->stream, dqDone * plane, dqEnd * plane);
-        });
-        dqDone = dqEnd;
-    }
+    if (seam && stage != this->state.template as<real>()) this->boundaryOn(stage);
+    this->launch("roe_delta_q_tilde", 1, [&] {
+        launchRoeDeltaQ<real>(this->rc.grid, stage, basis.template as<real>(), deltaQTilde.template as<real>(), seam,
+                              this->stream);
+    });
+}
+
+template <typename real>
+void Roe<real>::fluxPlanes(real* stage, long long from, long long to, cudaStream_t st) {
+    const Grid& g = this->rc.grid;
+    const long long plane = (long long)g.V / g.S[this->rc.dim - 1];
     if (to <= from) return;
     this->launch("roe_flux", sizeof(real) == 8 ? 2 : 1, [&] {
         launchRoeFlux<real>(g, this->rc.cfg.limiter, stage, basis.template as<real>(), deltaQTilde.template as<real>(),
-                            this->sc(), this->flux.template as<real>(), seam, this->stream, from * plane, to * plane);
+                            this->sc(), this->flux.template as<real>(), this->rc.cfg.compat == HGPU_COMPAT_SEAM, st,
+                            from * plane, to * plane);
     });
 }
 
@@ -1001,20 +1019,23 @@ void HLL<real>::step() {                                     // HLL::step (HLL.c
     });
 }
 
-// the flux of faces of slow-axis planes [from, to) (each reads the stage's planes q-1, q
-// and the wave speeds of plane q)
+// calcFlux in two parts: the ghost refresh (SEAM), then the flux of the faces of
+// slow-axis planes [from, to) on stream st (each reads the stage's planes q-1, q and the
+// wave speeds of plane q)
 template <typename real>
-void HLL<real>::fluxPlanes(real* stage, long long from, long long to, long long& dqDone) {
-    (void)dqDone;
+void HLL<real>::fluxPrepare(real* stage) {
+    if (this->rc.cfg.compat == HGPU_COMPAT_SEAM && stage != this->state.template as<real>()) this->boundaryOn(stage);
+}
+
+template <typename real>
+void HLL<real>::fluxPlanes(real* stage, long long from, long long to, cudaStream_t st) {
     const Grid& g = this->rc.grid;
     const long long plane = (long long)g.V / g.S[this->rc.dim - 1];
-    if (from == 0 && this->rc.cfg.compat == HGPU_COMPAT_SEAM && stage != this->state.template as<real>())
-        this->boundaryOn(stage);
     if (to <= from) return;
     this->launch("hllc_flux", 1, [&] {
         launchHllcFlux<real>(g, this->ph, stage, waves.template as<real>(), this->flux.template as<real>(),
-                             this->health, this->rc.cfg.solver == HGPU_SOLVER_HLL, this->stream,
-                             this->livePotential(), from * plane, to * plane);
+                             this->health, this->rc.cfg.solver == HGPU_SOLVER_HLL, st, this->livePotential(),
+                             from * plane, to * plane);
     });
 }
 

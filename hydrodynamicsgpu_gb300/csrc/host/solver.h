@@ -290,19 +290,22 @@ protected:
     virtual void bandedPrologueEnd() {}
     // the stages run as fused kernels (no separate combine to cut in bands)
     virtual bool fusedActive() const { return false; }
-    // The interface fluxes of `stage` on the faces of slow-axis planes [from, to), the
-    // same values calcFlux leaves for the whole grid; called for consecutive ranges from
-    // plane 0 (EulerRoe also forms the Delta-q-tilde planes they read, continuing from
-    // dqDone).  hostStep runs the last stage this way, band by band.
+    // calcFlux in two parts, so that hostStep can run the last stage band by band:
+    // fluxPrepare (on the solver's stream) does what precedes the fluxes for the whole
+    // grid (EulerRoe: the ghost refresh of SEAM, Delta-q-tilde), then fluxPlanes the
+    // interface fluxes of the faces of slow-axis planes [from, to) on stream `st`; the
+    // ranges' union gives the same values as calcFlux.
     virtual bool fluxByPlanes() const { return false; }
-    virtual void fluxPlanes(real* stage, long long from, long long to, long long& dqDone) {
-        (void)stage; (void)from; (void)to; (void)dqDone;
+    virtual void fluxPrepare(real* stage) { (void)stage; }
+    virtual void fluxPlanes(real* stage, long long from, long long to, cudaStream_t st) {
+        (void)stage; (void)from; (void)to; (void)st;
     }
 
 private:
     cudaStream_t copyStream_ = nullptr;     // update_host's uploads and downloads
-    cudaStream_t prepStream_ = nullptr;     // update_host: the bands' preparation as they land
-    cudaStream_t sideStream_ = nullptr;     // update_host: every other band's eigenbasis, the last combines
+    cudaStream_t prepStream_ = nullptr;     // update_host, high priority: the bands' preparation as they
+                                            // land, the last stage's band combines
+    cudaStream_t sideStream_ = nullptr;     // update_host: every other band's eigenbasis and last-stage fluxes
     std::vector<cudaEvent_t> pipeEvents_;
     cudaEvent_t pipeEvent(size_t i);
 };
@@ -338,7 +341,8 @@ protected:
     void bandedPrologueWork(int tile0, int tiles, cudaStream_t st) override;
     void bandedPrologueEnd() override { cflReduce(); }
     bool fluxByPlanes() const override { return true; }
-    void fluxPlanes(real* stage, long long from, long long to, long long& dqDone) override;
+    void fluxPrepare(real* stage) override;
+    void fluxPlanes(real* stage, long long from, long long to, cudaStream_t st) override;
 public:
     int setFusedStages(bool on) override;
 };
@@ -368,7 +372,8 @@ protected:
     void bandedPrologueWork(int tile0, int tiles, cudaStream_t st) override;
     void bandedPrologueEnd() override { calcTimestep(); }
     bool fluxByPlanes() const override { return true; }
-    void fluxPlanes(real* stage, long long from, long long to, long long& dqDone) override;
+    void fluxPrepare(real* stage) override;
+    void fluxPlanes(real* stage, long long from, long long to, cudaStream_t st) override;
 };
 
 template <typename real>
