@@ -59,6 +59,28 @@ __global__ void __launch_bounds__(kThreads) hllcFluxKernel(Grid g, Phys<real> ph
         atomicOr(health, HEALTH_HLLC_NOBRANCH);
 }
 
+// the flux with each cell's primitives staged once per tile (hllc_cells.cuh
+// hllcFluxTile), for slow-axis planes [s0, s1) (y in 2D, z in 3D)
+template <int D> struct FluxTile;
+template <> struct FluxTile<2> { enum { X = 32, Y = 8, Z = 1 }; };
+template <> struct FluxTile<3> { enum { X = 32, Y = 4, Z = 2 }; };
+
+template <typename real, int D, bool HLL, bool GRAV>
+__global__ void __launch_bounds__(kThreads) hllcFluxTileKernel(Grid g, Phys<real> ph, const real* __restrict__ stage,
+                                                               const real* __restrict__ waves,
+                                                               real* __restrict__ flux, unsigned* health,
+                                                               const real* __restrict__ pot, int s0, int s1) {
+    typedef FluxTile<D> T;
+    constexpr int HX = T::X + 1, HY = T::Y + 1, HZ = D > 2 ? T::Z + 1 : 1;
+    __shared__ Prim<real, D> prim[HX * HY * HZ];
+    const int x0 = blockIdx.x * T::X;
+    const int y0 = D == 2 ? s0 + (int)blockIdx.y * T::Y : (int)blockIdx.y * T::Y;
+    const int z0 = D == 2 ? 0 : s0 + (int)blockIdx.z * T::Z;
+    const bool ok = hllcFluxTile<real, D, HLL, GRAV>(g, ph, stage, waves, flux, x0, y0, z0, T::X, T::Y, T::Z, s0, s1,
+                                                     prim, pot);
+    if (!ok) atomicOr(health, HEALTH_HLLC_NOBRANCH);
+}
+
 }  // namespace
 
 // pot: the gravitational potential, or null for a zero potential
@@ -104,6 +126,29 @@ void launchHllcFluxG(const Grid& g, const Phys<real>& ph, const real* stage, con
                      unsigned* health, int hll, cudaStream_t st, const real* pot, long long c0, long long c1) {
     if (c1 < 0) c1 = g.V;
     if (c1 <= c0) return;
+    // 2D and 3D: the tile kernel over whole slow-axis planes
+    const long long plane = g.dim > 1 ? (long long)g.V / g.S[g.dim - 1] : 0;
+    if (g.dim > 1 && c0 % plane == 0 && c1 % plane == 0) {
+        const int s0 = (int)(c0 / plane), s1 = (int)(c1 / plane);
+#define T(DD, H)                                                                                                  \
+    {                                                                                                             \
+        typedef FluxTile<DD> FT;                                                                                  \
+        dim3 grid((unsigned)((g.S[0] + FT::X - 1) / FT::X),                                                       \
+                  (unsigned)(DD == 2 ? (s1 - s0 + FT::Y - 1) / FT::Y : (g.S[1] + FT::Y - 1) / FT::Y),             \
+                  (unsigned)(DD == 2 ? 1 : (s1 - s0 + FT::Z - 1) / FT::Z));                                        \
+        hllcFluxTileKernel<real, DD, H, GRAV><<<grid, kThreads, 0, st>>>(g, ph, stage, waves, flux, health, pot,  \
+                                                                          s0, s1);                                \
+    }
+        if (hll) {
+            if (g.dim == 2) T(2, true)
+            else T(3, true)
+        } else {
+            if (g.dim == 2) T(2, false)
+            else T(3, false)
+        }
+#undef T
+        return;
+    }
 #define L(DD, H)                                                                                                  \
     hllcFluxKernel<real, DD, H, GRAV><<<blocksFor(c1 - c0), kThreads, 0, st>>>(g, ph, stage, waves, flux, health, pot, \
                                                                              c0, c1)

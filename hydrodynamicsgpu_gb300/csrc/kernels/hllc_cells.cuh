@@ -18,6 +18,20 @@ struct Prim {
     real density, invDensity, v[3], velocitySq, energyTotal, pressure, enthalpyTotal, potential;
 };
 
+// the part of primitives() that follows the velocities: |v|^2 (components in order),
+// the internal energy, pressure and total enthalpy
+template <typename real, int D, bool GRAV = false>
+__device__ __forceinline__ void primitivesFromVelocity(real gamma, Prim<real, D>& p) {
+    p.velocitySq = mulI(p.v[0], p.v[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + mulI(p.v[k], p.v[k]);
+    real energyKinetic = halfOf(p.velocitySq);                          // .5f * velocitySq
+    real energyInternal = p.energyTotal - energyKinetic;
+    if (GRAV) energyInternal = energyInternal - p.potential;
+    p.pressure = (real)mulI(mulI((double)gamma - 1., (double)p.density), (double)energyInternal);
+    p.enthalpyTotal = p.energyTotal + mulI(p.pressure, p.invDensity);
+}
+
 // primitive variables of a rotated state (EulerHLLC.cl:54-64 / :218-238).  GRAV: with
 // the cell's potential phi (energyInternal = energyTotal - energyKinetic - phi);
 // otherwise the potential is zero and that term, which would change no bit, is left out.
@@ -30,16 +44,24 @@ __device__ __forceinline__ void primitives(const real* st, real gamma, Prim<real
     // VELOCITY: m/rho, by the correction step on RN(1/rho) in FP64 (fp64ops.cuh)
 #pragma unroll
     for (int k = 0; k < D; ++k) p.v[k] = divByRecip(st[1 + k], p.density, p.invDensity);
-    p.velocitySq = mulI(p.v[0], p.v[0]);
-#pragma unroll
-    for (int k = 1; k < D; ++k) p.velocitySq = p.velocitySq + mulI(p.v[k], p.v[k]);
     p.energyTotal = mulI(st[E], p.invDensity);
-    real energyKinetic = halfOf(p.velocitySq);                          // .5f * velocitySq
-    real energyInternal = p.energyTotal - energyKinetic;
-    if (GRAV) energyInternal = energyInternal - phi;
     p.potential = phi;
-    p.pressure = (real)mulI(mulI((double)gamma - 1., (double)p.density), (double)energyInternal);
-    p.enthalpyTotal = p.energyTotal + mulI(p.pressure, p.invDensity);
+    primitivesFromVelocity<real, D, GRAV>(gamma, p);
+}
+
+// a face's primitives from its cell's, staged unrotated (hllcFluxTile): the velocities
+// permuted as loadRotated permutes the momenta.  |v|^2 sums the rotated components in
+// order; it changes only where the rotation moves the last component (3D, SIDE 2: v_z
+// first), and there |v|^2, pressure and enthalpy are formed again from the rotated
+// velocities, so every value is what primitives() gives for the rotated state.
+template <typename real, int D, int SIDE, bool GRAV = false>
+__device__ __forceinline__ void rotatePrim(const Prim<real, D>& p, real gamma, Prim<real, D>& r) {
+    r = p;
+    if (SIDE > 0) {
+        r.v[0] = p.v[SIDE];
+        r.v[SIDE] = p.v[0];
+    }
+    if (D == 3 && SIDE == 2) primitivesFromVelocity<real, D, GRAV>(gamma, r);
 }
 
 // sl, sr of one face (EulerHLLC.cl:85-97)
@@ -145,12 +167,23 @@ __device__ __forceinline__ unsigned long long hllcDtCell(const Grid& g, const Ph
     return realBits(result);
 }
 
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllcFaceFromPrim(const Grid& g, const real* stL, const real* stR,
+                                                 const Prim<real, D>& L, const Prim<real, D>& R,
+                                                 const real* __restrict__ waves, real* __restrict__ fluxBuf,
+                                                 long long c);
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllFaceFromPrim(const Grid& g, const real* stL, const real* stR,
+                                                const Prim<real, D>& L, const Prim<real, D>& R,
+                                                const real* __restrict__ waves, real* __restrict__ fluxBuf,
+                                                long long c);
+
 // HLLC flux, HLLC_METHOD 2 (EulerHLLC.cl:240-418); `flux` holds the face's previous value.
 template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
                                          const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c,
         const real* __restrict__ pot = nullptr) {
-    const int N = D + 2, E = N - 1;
+    const int N = D + 2;
     if (!cellOk(g, c) || !cellOk(g, c - g.step[SIDE])) return true;
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
@@ -158,6 +191,16 @@ __device__ __forceinline__ bool hllcFace(const Grid& g, const Phys<real>& ph, co
     Prim<real, D> L, R;
     primitives<real, D, GRAV>(stL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
     primitives<real, D, GRAV>(stR, ph.gamma, R, GRAV ? pot[c] : (real)0);
+    return hllcFaceFromPrim<real, D, SIDE>(g, stL, stR, L, R, waves, fluxBuf, c);
+}
+
+// the rest of hllcFace, given the face's rotated states and their primitives
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllcFaceFromPrim(const Grid& g, const real* stL, const real* stR,
+                                                 const Prim<real, D>& L, const Prim<real, D>& R,
+                                                 const real* __restrict__ waves, real* __restrict__ fluxBuf,
+                                                 long long c) {
+    const int N = D + 2, E = N - 1;
     real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
     real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
     real fL[N], fR[N], flux[N];
@@ -220,7 +263,7 @@ template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
                                         const real* __restrict__ waves, real* __restrict__ fluxBuf, long long c,
         const real* __restrict__ pot = nullptr) {
-    const int N = D + 2, E = N - 1;
+    const int N = D + 2;
     if (!cellOk(g, c) || !cellOk(g, c - g.step[SIDE])) return true;
     real stL[N], stR[N];
     loadRotated<real, D, SIDE>(stage, c - g.step[SIDE], stL);
@@ -228,6 +271,16 @@ __device__ __forceinline__ bool hllFace(const Grid& g, const Phys<real>& ph, con
     Prim<real, D> L, R;
     primitives<real, D, GRAV>(stL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
     primitives<real, D, GRAV>(stR, ph.gamma, R, GRAV ? pot[c] : (real)0);
+    return hllFaceFromPrim<real, D, SIDE>(g, stL, stR, L, R, waves, fluxBuf, c);
+}
+
+// the rest of hllFace, given the face's rotated states and their primitives
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ bool hllFaceFromPrim(const Grid& g, const real* stL, const real* stR,
+                                                const Prim<real, D>& L, const Prim<real, D>& R,
+                                                const real* __restrict__ waves, real* __restrict__ fluxBuf,
+                                                long long c) {
+    const int N = D + 2, E = N - 1;
     const real sl = waves[((long long)SIDE * 2 + 0) * g.V + c];
     const real sr = waves[((long long)SIDE * 2 + 1) * g.V + c];
     real fL[N], fR[N], flux[N];
@@ -292,6 +345,84 @@ __device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph
             else ok &= hllcFace<real, D, (D > 2 ? 2 : 0), GRAV>(g, ph, stage, waves, flux, c, pot);
         }
     }
+    return ok;
+}
+
+// The HLLC (HLL) fluxes of a tile of cells with each cell's primitives formed once:
+// the tile plus one cell below along every axis (each face's left cell) is staged in
+// `prim` (HX*HY*HZ entries), then each cell takes its faces as hllcFluxCell does, the
+// primitives rotated to the face (rotatePrim) instead of formed from the rotated
+// state (every face otherwise formed its two cells' primitives).  Cells with slow-axis
+// coordinate outside [s0, s1) (y in 2D, z in 3D) are staged only.  Returns through
+// `ok` whether every face took a flux branch.
+template <typename real, int D, bool HLL = false, bool GRAV = false>
+__device__ __forceinline__ bool hllcFluxTile(const Grid& g, const Phys<real>& ph, const real* __restrict__ stage,
+                                             const real* __restrict__ waves, real* __restrict__ flux, int x0, int y0,
+                                             int z0, int TX, int TY, int TZ, int s0, int s1, Prim<real, D>* prim,
+                                             const real* __restrict__ pot = nullptr) {
+    const int N = D + 2;
+    const int HX = TX + 1, HY = D > 1 ? TY + 1 : 1, HZ = D > 2 ? TZ + 1 : 1;
+    const int ox = 1, oy = D > 1 ? 1 : 0, oz = D > 2 ? 1 : 0;
+    for (int i = threadIdx.x; i < HX * HY * HZ; i += blockDim.x) {
+        int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
+        int gx = x0 - ox + hx, gy = y0 - oy + hy, gz = z0 - oz + hz;
+        if (gx >= 0 && gx < g.S[0] && gy >= 0 && gy < g.S[1] && gz >= 0 && gz < g.S[2]) {
+            long long c = gx + (long long)g.S[0] * (gy + (long long)g.S[1] * gz);
+            if (cellOk(g, c)) {
+                real s[N];
+#pragma unroll
+                for (int j = 0; j < N; ++j) s[j] = stage[(long long)N * c + j];
+                primitives<real, D, GRAV>(s, ph.gamma, prim[i], GRAV ? pot[c] : (real)0);
+            }
+        }
+    }
+    __syncthreads();
+    bool ok = true;
+    const int tx = threadIdx.x % TX, ty = (threadIdx.x / TX) % TY, tz = threadIdx.x / (TX * TY);
+    const int x = x0 + tx, y = y0 + ty, z = z0 + tz;
+    const int slow = D == 2 ? y : z;
+    if (tz < TZ && x < g.S[0] && y < g.S[1] && z < g.S[2] && slow >= s0 && slow < s1) {
+        const long long c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
+        const int self = (tz + oz) * HY * HX + (ty + oy) * HX + (tx + ox);
+        const int cc[3] = {x, y, z};
+        const int below[3] = {1, HX, HX * HY};
+#pragma unroll
+        for (int side = 0; side < D; ++side) {
+            bool in = true;
+            for (int a = 0; a < D; ++a) {
+                int hi = a == side ? 1 : 2;
+                if (cc[a] < 2 || cc[a] >= g.S[a] - hi) in = false;
+            }
+            if (!in || !cellOk(g, c) || !cellOk(g, c - g.step[side])) continue;
+            real stL[N], stR[N];
+            Prim<real, D> L, R;
+            if (side == 0) {
+                loadRotated<real, D, 0>(stage, c - g.step[0], stL);
+                loadRotated<real, D, 0>(stage, c, stR);
+                rotatePrim<real, D, 0, GRAV>(prim[self - below[0]], ph.gamma, L);
+                rotatePrim<real, D, 0, GRAV>(prim[self], ph.gamma, R);
+                ok &= HLL ? hllFaceFromPrim<real, D, 0>(g, stL, stR, L, R, waves, flux, c)
+                          : hllcFaceFromPrim<real, D, 0>(g, stL, stR, L, R, waves, flux, c);
+            } else if (side == 1) {
+                constexpr int S1 = D > 1 ? 1 : 0;
+                loadRotated<real, D, S1>(stage, c - g.step[1], stL);
+                loadRotated<real, D, S1>(stage, c, stR);
+                rotatePrim<real, D, S1, GRAV>(prim[self - below[1]], ph.gamma, L);
+                rotatePrim<real, D, S1, GRAV>(prim[self], ph.gamma, R);
+                ok &= HLL ? hllFaceFromPrim<real, D, S1>(g, stL, stR, L, R, waves, flux, c)
+                          : hllcFaceFromPrim<real, D, S1>(g, stL, stR, L, R, waves, flux, c);
+            } else {
+                constexpr int S2 = D > 2 ? 2 : 0;
+                loadRotated<real, D, S2>(stage, c - g.step[2], stL);
+                loadRotated<real, D, S2>(stage, c, stR);
+                rotatePrim<real, D, S2, GRAV>(prim[self - below[2]], ph.gamma, L);
+                rotatePrim<real, D, S2, GRAV>(prim[self], ph.gamma, R);
+                ok &= HLL ? hllFaceFromPrim<real, D, S2>(g, stL, stR, L, R, waves, flux, c)
+                          : hllcFaceFromPrim<real, D, S2>(g, stL, stR, L, R, waves, flux, c);
+            }
+        }
+    }
+    __syncthreads();
     return ok;
 }
 
