@@ -81,7 +81,30 @@ __global__ void __launch_bounds__(kThreads) hllcFluxTileKernel(Grid g, Phys<real
     if (!ok) atomicOr(health, HEALTH_HLLC_NOBRANCH);
 }
 
+template <typename real, int D, bool HLL, bool GRAV>
+__global__ void __launch_bounds__(kThreads) hllcWaveTileKernel(Grid g, Phys<real> ph, double gq,
+                                                               const real* __restrict__ state,
+                                                               real* __restrict__ waves, const real* __restrict__ pot,
+                                                               int s0, int s1) {
+    typedef FluxTile<D> T;
+    constexpr int HX = T::X + 1, HY = T::Y + 1, HZ = D > 2 ? T::Z + 1 : 1;
+    __shared__ Prim<real, D> prim[HX * HY * HZ];
+    const int x0 = blockIdx.x * T::X;
+    const int y0 = D == 2 ? s0 + (int)blockIdx.y * T::Y : (int)blockIdx.y * T::Y;
+    const int z0 = D == 2 ? 0 : s0 + (int)blockIdx.z * T::Z;
+    hllcWaveTile<real, D, HLL, GRAV>(g, ph, gq, state, waves, x0, y0, z0, T::X, T::Y, T::Z, s0, s1, prim, pot);
+}
+
 }  // namespace
+
+// the grid of a tile kernel over slow-axis planes [s0, s1)
+template <int D>
+static dim3 tileGrid(const Grid& g, int s0, int s1) {
+    typedef FluxTile<D> FT;
+    return dim3((unsigned)((g.S[0] + FT::X - 1) / FT::X),
+                (unsigned)(D == 2 ? (s1 - s0 + FT::Y - 1) / FT::Y : (g.S[1] + FT::Y - 1) / FT::Y),
+                (unsigned)(D == 2 ? 1 : (s1 - s0 + FT::Z - 1) / FT::Z));
+}
 
 // pot: the gravitational potential, or null for a zero potential
 template <typename real, bool GRAV>
@@ -92,6 +115,22 @@ void launchHllcWavesG(const Grid& g, const Phys<real>& ph, const real* state, re
     if (c0 >= c1) return;
     // (gamma + 1.) / (2. * gamma) is a per-program constant (double literals); computed once, identically
     double gq = ((double)ph.gamma + 1.) / (2. * (double)ph.gamma);
+    // 2D and 3D: the staged tile kernel over whole slow-axis planes
+    const long long plane = g.dim > 1 ? (long long)g.V / g.S[g.dim - 1] : 0;
+    if (g.dim > 1 && c0 % plane == 0 && c1 % plane == 0) {
+        const int s0 = (int)(c0 / plane), s1 = (int)(c1 / plane);
+#define T(DD, H) \
+    hllcWaveTileKernel<real, DD, H, GRAV><<<tileGrid<DD>(g, s0, s1), kThreads, 0, st>>>(g, ph, gq, state, waves, pot, s0, s1)
+        if (hll) {
+            if (g.dim == 2) T(2, true);
+            else T(3, true);
+        } else {
+            if (g.dim == 2) T(2, false);
+            else T(3, false);
+        }
+#undef T
+        return;
+    }
 #define L(DD, H) \
     hllcWaveKernel<real, DD, H, GRAV><<<blocksFor(c1 - c0), kThreads, 0, st>>>(g, ph, gq, state, waves, pot, c0, c1)
     if (hll) {

@@ -65,6 +65,14 @@ __device__ __forceinline__ void rotatePrim(const Prim<real, D>& p, real gamma, P
 }
 
 // sl, sr of one face (EulerHLLC.cl:85-97)
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void waveFaceFromPrim(const Grid& g, const Phys<real>& ph, double gq,
+                                                 const Prim<real, D>& L, const Prim<real, D>& R,
+                                                 real* __restrict__ waves, long long c);
+template <typename real, int D, int SIDE, bool GRAV>
+__device__ __forceinline__ void hllWaveFaceFromPrim(const Grid& g, const Phys<real>& ph, const Prim<real, D>& L,
+                                                    const Prim<real, D>& R, real* __restrict__ waves, long long c);
+
 template <typename real, int D, int SIDE, bool GRAV = false>
 __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, double gq, const real* __restrict__ state,
                                          real* __restrict__ waves, long long c,
@@ -73,10 +81,18 @@ __device__ __forceinline__ void waveFace(const Grid& g, const Phys<real>& ph, do
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
-    const double gm1 = (double)ph.gamma - 1.;
     Prim<real, D> L, R;
     primitives<real, D, GRAV>(sL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
     primitives<real, D, GRAV>(sR, ph.gamma, R, GRAV ? pot[c] : (real)0);
+    waveFaceFromPrim<real, D, SIDE>(g, ph, gq, L, R, waves, c);
+}
+
+// the rest of waveFace, given the face's two cells' primitives (rotated to the face)
+template <typename real, int D, int SIDE>
+__device__ __forceinline__ void waveFaceFromPrim(const Grid& g, const Phys<real>& ph, double gq,
+                                                 const Prim<real, D>& L, const Prim<real, D>& R,
+                                                 real* __restrict__ waves, long long c) {
+    const double gm1 = (double)ph.gamma - 1.;
     real cL = (real)sqrt(mulI(gm1, (double)(L.enthalpyTotal - halfOf(L.velocitySq))));
     real cR = (real)sqrt(mulI(gm1, (double)(R.enthalpyTotal - halfOf(R.velocitySq))));
     // .5f * (pL + pR) - .5f * (vR - vL) * .5f * (rhoL + rhoR) * .5f * (cL + cR), halvings exact
@@ -103,10 +119,17 @@ __device__ __forceinline__ void hllWaveFace(const Grid& g, const Phys<real>& ph,
     real sL[D + 2], sR[D + 2];
     loadRotated<real, D, SIDE>(state, c - g.step[SIDE], sL);
     loadRotated<real, D, SIDE>(state, c, sR);
-    const double gm1 = (double)ph.gamma - 1.;
     Prim<real, D> L, R;
     primitives<real, D, GRAV>(sL, ph.gamma, L, GRAV ? pot[c - g.step[SIDE]] : (real)0);
     primitives<real, D, GRAV>(sR, ph.gamma, R, GRAV ? pot[c] : (real)0);
+    hllWaveFaceFromPrim<real, D, SIDE, GRAV>(g, ph, L, R, waves, c);
+}
+
+// the rest of hllWaveFace, given the face's two cells' primitives (rotated to the face)
+template <typename real, int D, int SIDE, bool GRAV>
+__device__ __forceinline__ void hllWaveFaceFromPrim(const Grid& g, const Phys<real>& ph, const Prim<real, D>& L,
+                                                    const Prim<real, D>& R, real* __restrict__ waves, long long c) {
+    const double gm1 = (double)ph.gamma - 1.;
     const real cL = (real)sqrt(mulI(gm1, (double)L.enthalpyTotal - halfOf((double)L.velocitySq)));
     const real cR = (real)sqrt(mulI(gm1, (double)R.enthalpyTotal - halfOf((double)R.velocitySq)));
     const real wL = sqrt(L.density), wR = sqrt(R.density);
@@ -348,6 +371,75 @@ __device__ __forceinline__ bool hllcFluxCell(const Grid& g, const Phys<real>& ph
     return ok;
 }
 
+// primitives of the tile's cells and of one cell below along every axis, into `prim`
+// (HX*HY*HZ entries, x fastest); the caller synchronises
+template <typename real, int D, bool GRAV>
+__device__ __forceinline__ void stagePrims(const Grid& g, const Phys<real>& ph, const real* __restrict__ st,
+                                           int x0, int y0, int z0, int HX, int HY, int HZ, Prim<real, D>* prim,
+                                           const real* __restrict__ pot) {
+    const int N = D + 2;
+    const int ox = 1, oy = D > 1 ? 1 : 0, oz = D > 2 ? 1 : 0;
+    for (int i = threadIdx.x; i < HX * HY * HZ; i += blockDim.x) {
+        int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
+        int gx = x0 - ox + hx, gy = y0 - oy + hy, gz = z0 - oz + hz;
+        if (gx >= 0 && gx < g.S[0] && gy >= 0 && gy < g.S[1] && gz >= 0 && gz < g.S[2]) {
+            long long c = gx + (long long)g.S[0] * (gy + (long long)g.S[1] * gz);
+            if (cellOk(g, c)) {
+                real s[N];
+#pragma unroll
+                for (int j = 0; j < N; ++j) s[j] = st[(long long)N * c + j];
+                primitives<real, D, GRAV>(s, ph.gamma, prim[i], GRAV ? pot[c] : (real)0);
+            }
+        }
+    }
+}
+
+// The wave speeds of a tile's cells' faces (hllcWaveCell) with each cell's primitives
+// formed once and rotated to each face (rotatePrim), as hllcFluxTile does for the flux.
+// Cells with slow-axis coordinate outside [s0, s1) are staged only.
+template <typename real, int D, bool HLL = false, bool GRAV = false>
+__device__ __forceinline__ void hllcWaveTile(const Grid& g, const Phys<real>& ph, double gq,
+                                             const real* __restrict__ state, real* __restrict__ waves, int x0, int y0,
+                                             int z0, int TX, int TY, int TZ, int s0, int s1, Prim<real, D>* prim,
+                                             const real* __restrict__ pot = nullptr) {
+    const int HX = TX + 1, HY = D > 1 ? TY + 1 : 1, HZ = D > 2 ? TZ + 1 : 1;
+    const int ox = 1, oy = D > 1 ? 1 : 0, oz = D > 2 ? 1 : 0;
+    stagePrims<real, D, GRAV>(g, ph, state, x0, y0, z0, HX, HY, HZ, prim, pot);
+    __syncthreads();
+    const int tx = threadIdx.x % TX, ty = (threadIdx.x / TX) % TY, tz = threadIdx.x / (TX * TY);
+    const int x = x0 + tx, y = y0 + ty, z = z0 + tz;
+    const int slow = D == 2 ? y : z;
+    if (tz < TZ && x < g.S[0] && y < g.S[1] && z < g.S[2] && slow >= s0 && slow < s1 && inRange(g, x, y, z, 2, 1)) {
+        const long long c = x + (long long)g.S[0] * (y + (long long)g.S[1] * z);
+        const int self = (tz + oz) * HY * HX + (ty + oy) * HX + (tx + ox);
+        const int below[3] = {1, HX, HX * HY};
+#pragma unroll
+        for (int side = 0; side < D; ++side) {
+            if (!cellOk(g, c) || !cellOk(g, c - g.step[side])) continue;
+            Prim<real, D> L, R;
+            if (side == 0) {
+                rotatePrim<real, D, 0, GRAV>(prim[self - below[0]], ph.gamma, L);
+                rotatePrim<real, D, 0, GRAV>(prim[self], ph.gamma, R);
+                if (HLL) hllWaveFaceFromPrim<real, D, 0, GRAV>(g, ph, L, R, waves, c);
+                else waveFaceFromPrim<real, D, 0>(g, ph, gq, L, R, waves, c);
+            } else if (side == 1) {
+                constexpr int S1 = D > 1 ? 1 : 0;
+                rotatePrim<real, D, S1, GRAV>(prim[self - below[1]], ph.gamma, L);
+                rotatePrim<real, D, S1, GRAV>(prim[self], ph.gamma, R);
+                if (HLL) hllWaveFaceFromPrim<real, D, S1, GRAV>(g, ph, L, R, waves, c);
+                else waveFaceFromPrim<real, D, S1>(g, ph, gq, L, R, waves, c);
+            } else {
+                constexpr int S2 = D > 2 ? 2 : 0;
+                rotatePrim<real, D, S2, GRAV>(prim[self - below[2]], ph.gamma, L);
+                rotatePrim<real, D, S2, GRAV>(prim[self], ph.gamma, R);
+                if (HLL) hllWaveFaceFromPrim<real, D, S2, GRAV>(g, ph, L, R, waves, c);
+                else waveFaceFromPrim<real, D, S2>(g, ph, gq, L, R, waves, c);
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // The HLLC (HLL) fluxes of a tile of cells with each cell's primitives formed once:
 // the tile plus one cell below along every axis (each face's left cell) is staged in
 // `prim` (HX*HY*HZ entries), then each cell takes its faces as hllcFluxCell does, the
@@ -363,19 +455,7 @@ __device__ __forceinline__ bool hllcFluxTile(const Grid& g, const Phys<real>& ph
     const int N = D + 2;
     const int HX = TX + 1, HY = D > 1 ? TY + 1 : 1, HZ = D > 2 ? TZ + 1 : 1;
     const int ox = 1, oy = D > 1 ? 1 : 0, oz = D > 2 ? 1 : 0;
-    for (int i = threadIdx.x; i < HX * HY * HZ; i += blockDim.x) {
-        int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
-        int gx = x0 - ox + hx, gy = y0 - oy + hy, gz = z0 - oz + hz;
-        if (gx >= 0 && gx < g.S[0] && gy >= 0 && gy < g.S[1] && gz >= 0 && gz < g.S[2]) {
-            long long c = gx + (long long)g.S[0] * (gy + (long long)g.S[1] * gz);
-            if (cellOk(g, c)) {
-                real s[N];
-#pragma unroll
-                for (int j = 0; j < N; ++j) s[j] = stage[(long long)N * c + j];
-                primitives<real, D, GRAV>(s, ph.gamma, prim[i], GRAV ? pot[c] : (real)0);
-            }
-        }
-    }
+    stagePrims<real, D, GRAV>(g, ph, stage, x0, y0, z0, HX, HY, HZ, prim, pot);
     __syncthreads();
     bool ok = true;
     const int tx = threadIdx.x % TX, ty = (threadIdx.x / TX) % TY, tz = threadIdx.x / (TX * TY);
