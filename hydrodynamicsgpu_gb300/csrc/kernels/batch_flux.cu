@@ -59,8 +59,8 @@ __global__ void __launch_bounds__(256) batchFluxCorrKernel(const BatchProblem<do
             int x, y, z;
             long long c;
             if (!tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c)) continue;
-            roeFluxCorrectionsCell<D, LIM>(g, lim, sc[tl.p], faces + pr.faceOff, dq + pr.dqOff, flux + pr.dqOff, c, x,
-                                           y, z);
+            roeFluxCorrectionsCell<D, LIM, false, true>(g, lim, sc[tl.p], faces + pr.faceOff, dq + pr.dqOff,
+                                                        flux + pr.dqOff, c, x, y, z);
         }
     }
 }

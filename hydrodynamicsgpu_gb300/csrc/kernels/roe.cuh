@@ -350,7 +350,13 @@ __device__ __forceinline__ void roeFlux(const real* rec, const real* sL, const r
 // Each pass keeps far fewer values live than the fused form, so more warps fit per SM.
 // REC also stores the per-wave tape values of this pass (A, phi, phi', r; the caller
 // offsets tape to the face, as for roeFlux).
-template <int D, int SIDE, int LIM, bool REC = false>
+// FLATQ: a wave whose Delta-q-tilde is +-0, with finite lambda and A, gets its
+// correction (lambda (+-0) / 2) A as the signed zero it is (sign(lambda) xor sign(dq)
+// xor sign(A)) on the bit patterns, skipping the product's and the halving's
+// out-of-line FP64 calls for zero operands.  Piecewise-constant states (the batched
+// four-quadrant problems) have such waves on most faces; the KH step measured it
+// slower, so it is the batched kernel's choice.
+template <int D, int SIDE, int LIM, bool REC = false, bool FLATQ = false>
 __device__ __forceinline__ void roeFluxCorrections(const double* rec, const double* dqL, const double* dq,
                                                    const double* dqR, double dt_dx, int lim, double* corr,
                                                    double* __restrict__ tape = nullptr, long long V = 0) {
@@ -370,7 +376,10 @@ __device__ __forceinline__ void roeFluxCorrections(const double* rec, const doub
         const double phi = slopeLimiter<double>(LIM >= 0 ? LIM : lim, rTilde);
         const double epsMinusTheta = mid ? midEpsTheta : mulI(eigenvalue, dt_dx) - theta;
         const double A = theta + phi * epsMinusTheta;
-        corr[i] = halfOf(mulI(eigenvalue, dq[i])) * A;
+        if (FLATQ && isZeroBits(dq[i]) && finiteD(eigenvalue) && finiteD(A))
+            corr[i] = fromBits((bitsOf(eigenvalue) ^ bitsOf(dq[i]) ^ bitsOf(A)) & (long long)0x8000000000000000ULL);
+        else
+            corr[i] = halfOf(mulI(eigenvalue, dq[i])) * A;
         if (REC) {
             tape[((long long)FT_A * N + i) * V] = A;
             tape[((long long)FT_PHI * N + i) * V] = phi;

@@ -175,7 +175,7 @@ __device__ __forceinline__ void roeFluxCell(const Grid& g, int lim, const StepCo
 
 // the two passes of the split FP64 flux (roe.cuh) over the faces of one cell
 // (REC: tape planes per face as for roeFluxCell)
-template <int D, int LIM, bool REC = false>
+template <int D, int LIM, bool REC = false, bool FLATQ = false>
 __device__ __forceinline__ void roeFluxCorrectionsCell(const Grid& g, int lim, const StepConst<double>& sc,
                                                        const double* __restrict__ basis,
                                                        const double* __restrict__ dq, double* __restrict__ flux,
@@ -198,10 +198,10 @@ __device__ __forceinline__ void roeFluxCorrectionsCell(const Grid& g, int lim, c
             qR[i] = p[st];
         }
         double* tf = REC ? tape + (long long)side * FT_PLANES * N * g.V + c : nullptr;
-        if (side == 0) roeFluxCorrections<D, 0, LIM, REC>(rec, qL, q, qR, sc.dt_dx[0], lim, corr, tf, g.V);
+        if (side == 0) roeFluxCorrections<D, 0, LIM, REC, FLATQ>(rec, qL, q, qR, sc.dt_dx[0], lim, corr, tf, g.V);
         else if (side == 1)
-            roeFluxCorrections<D, (D > 1 ? 1 : 0), LIM, REC>(rec, qL, q, qR, sc.dt_dx[1], lim, corr, tf, g.V);
-        else roeFluxCorrections<D, (D > 2 ? 2 : 0), LIM, REC>(rec, qL, q, qR, sc.dt_dx[2], lim, corr, tf, g.V);
+            roeFluxCorrections<D, (D > 1 ? 1 : 0), LIM, REC, FLATQ>(rec, qL, q, qR, sc.dt_dx[1], lim, corr, tf, g.V);
+        else roeFluxCorrections<D, (D > 2 ? 2 : 0), LIM, REC, FLATQ>(rec, qL, q, qR, sc.dt_dx[2], lim, corr, tf, g.V);
 #pragma unroll
         for (int i = 0; i < N; ++i) flux[((long long)side * N + i) * g.V + c] = corr[i];
     }
