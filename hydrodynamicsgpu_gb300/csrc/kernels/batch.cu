@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256, PLAIN ? 5 : 1) batchCombineKernel(const B
         long long c;
         for (int r = 0; r < (PLAIN ? 1 : tu.cpt); ++r)
         if (tileCell(g, tl, tu, threadIdx.x + r * blockDim.x, x, y, z, c))
-            derivCombineCell<real, D, D>(g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
+            derivCombineCell<real, D, D, true>(g, pr.ph, flux + pr.dqOff, plan, sc[tl.p], c, x, y, z, pr.stateOff);
     }
 }
 

@@ -90,7 +90,17 @@ __device__ __forceinline__ void boundaryLine(const Grid& g, int axis, int N, int
     }
 }
 
-template <typename real, int D>
+// x * y for an x that is often +-0 (flux differences of piecewise-constant states):
+// the signed zero from the bit patterns when x is zero and y finite (what the product
+// gives), otherwise mulI, whose zero operands take an out-of-line FP64 call
+__device__ __forceinline__ double mulZ(double x, double y) {
+    if (isZeroBits(x) && finiteD(y)) return fromBits((bitsOf(x) ^ bitsOf(y)) & (long long)0x8000000000000000ULL);
+    return mulI(x, y);
+}
+__device__ __forceinline__ float mulZ(float x, float y) { return x * y; }
+
+// FLATD: the deriv's products by mulZ (the batched kernels, whose states are mostly flat)
+template <typename real, int D, bool FLATD = false>
 __device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan<real>& plan,
                                                 const StepConst<real>& sc, long long c, long long off);
 
@@ -101,7 +111,7 @@ __device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan
 // two FMAs) for the first RECIP_SIDES axes, on the integer pipes (divI) for the rest.
 // Measured: the single-problem kernel is fastest with 1 (0.357 ms a launch at 2048^2,
 // 0.390 with 0, 0.408 with every axis), the batched persistent one with every axis.
-template <typename real, int D, int RECIP_SIDES = 1>
+template <typename real, int D, int RECIP_SIDES = 1, bool FLATD = false>
 __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>& ph, const real* __restrict__ flux,
                                                  const CombinePlan<real>& plan, const StepConst<real>& sc,
                                                  long long c, int x, int y, int z, long long off) {
@@ -127,12 +137,12 @@ __device__ __forceinline__ void derivCombineCell(const Grid& g, const Phys<real>
 #pragma unroll
         for (int j = 0; j < N; ++j) d[j] = (real)0.;
     }
-    combinePlanCell<real, D>(d, plan, sc, c, off);
+    combinePlanCell<real, D, FLATD>(d, plan, sc, c, off);
 }
 
 // The integrator's use of one cell's deriv d: ForwardEuler's state += deriv * dt, or
 // this stage's column of the Runge-Kutta rows (see combine.cu).
-template <typename real, int D>
+template <typename real, int D, bool FLATD>
 __device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan<real>& plan,
                                                 const StepConst<real>& sc, long long c, long long off) {
     const int N = D + 2;
@@ -140,7 +150,7 @@ __device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan
         real dt = sc.dt;
         real* s = plan.slot[0] + (long long)N * (off + c);
 #pragma unroll
-        for (int j = 0; j < N; ++j) s[j] = s[j] + mulI(d[j], dt);
+        for (int j = 0; j < N; ++j) s[j] = s[j] + (FLATD ? mulZ(d[j], dt) : mulI(d[j], dt));
         return;
     }
     real u[N];
@@ -168,7 +178,7 @@ __device__ __forceinline__ void combinePlanCell(const real* d, const CombinePlan
             real cf = sc.coef[op.brow][op.bcol];
 #pragma unroll
             for (int j = 0; j < N; ++j) {
-                real t = mulI(d[j], cf);
+                real t = FLATD ? mulZ(d[j], cf) : mulI(d[j], cf);
                 v[j] = empty ? zfix(t) : v[j] + t;
             }
         }
