@@ -81,6 +81,25 @@ __global__ void __launch_bounds__(kThreads) hllcFluxTileKernel(Grid g, Phys<real
     if (!ok) atomicOr(health, HEALTH_HLLC_NOBRANCH);
 }
 
+// The same for 2D EulerHLLC with the register budget of one block per SM: ptxas then
+// keeps 102 registers (2 blocks per SM) instead of its default 80 (3 blocks), which
+// measured faster (KH 2048^2 RK4 8.32 -> 7.71 ms a step); EulerHLL and 3D measured
+// slower that way and keep the kernel above.
+template <typename real, bool GRAV>
+__global__ void __launch_bounds__(kThreads, 1) hllcFluxTileKernelWide(Grid g, Phys<real> ph,
+                                                                      const real* __restrict__ stage,
+                                                                      const real* __restrict__ waves,
+                                                                      real* __restrict__ flux, unsigned* health,
+                                                                      const real* __restrict__ pot, int s0, int s1) {
+    typedef FluxTile<2> T;
+    constexpr int HX = T::X + 1, HY = T::Y + 1;
+    __shared__ Prim<real, 2> prim[HX * HY];
+    const int x0 = blockIdx.x * T::X, y0 = s0 + (int)blockIdx.y * T::Y;
+    const bool ok = hllcFluxTile<real, 2, false, GRAV>(g, ph, stage, waves, flux, x0, y0, 0, T::X, T::Y, 1, s0, s1,
+                                                       prim, pot);
+    if (!ok) atomicOr(health, HEALTH_HLLC_NOBRANCH);
+}
+
 template <typename real, int D, bool HLL, bool GRAV>
 __global__ void __launch_bounds__(kThreads) hllcWaveTileKernel(Grid g, Phys<real> ph, double gq,
                                                                const real* __restrict__ state,
@@ -182,7 +201,10 @@ void launchHllcFluxG(const Grid& g, const Phys<real>& ph, const real* stage, con
             if (g.dim == 2) T(2, true)
             else T(3, true)
         } else {
-            if (g.dim == 2) T(2, false)
+            if (g.dim == 2)
+                hllcFluxTileKernelWide<real, GRAV><<<tileGrid<2>(g, s0, s1), kThreads, 0, st>>>(g, ph, stage, waves,
+                                                                                                flux, health, pot, s0,
+                                                                                                s1);
             else T(3, false)
         }
 #undef T
