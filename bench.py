@@ -549,10 +549,13 @@ MEASURED_TRAFFIC_PER_CELL = {"roe_flux": 568.0, "roe_delta_q_tilde": 252.0, "roe
 
 # Instructions the FP64 unit executes per interior cell of one launch of each kernel of
 # the EulerRoe FP64 step (MinMod), from ncu's smsp__inst_executed_pipe_fp64 (warp
-# instructions x 32) over the cells of a KH 512x512 step of the same kernels; roe_flux
-# is its two passes together (corrections 30.6 + transforms 65.5).
-FP64_PIPE_PER_CELL = {"roe_eigenbasis": 71.4, "cfl_min_reduce": 9.9, "roe_delta_q_tilde": 37.7,
-                      "roe_flux": 96.1, "flux_divergence_combine": 40.9, "state_check": 2.0}
+# instructions x 32) over the cells of the second of two KH 512x512 RK4 steps of the same
+# kernels; roe_flux is its two passes together (corrections 30.57 + transforms 65.55);
+# Delta-q-tilde and the combine vary by stage, so theirs are the step's means (Delta-q-
+# tilde 29.79 in every stage; the combine 40.87, 32.87, 32.87, 28.34).  763.1 per RK4
+# cell-update.
+FP64_PIPE_PER_CELL = {"roe_eigenbasis": 112.62, "cfl_min_reduce": 9.92, "roe_delta_q_tilde": 29.79,
+                      "roe_flux": 96.12, "flux_divergence_combine": 33.74, "state_check": 1.98}
 
 
 def fp64_roofline(prof, value, fp64_peak):
