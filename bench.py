@@ -457,6 +457,7 @@ def adjoint_measure(hg, _abi, ic, args):
     fwd_ms = bwd_ms = plain_ms = 0.
     tfwd_ms = tbwd_ms = 0.
     taped_same = True
+    taped_error = None
     fd = None
     for k in range(args.adjoint_problems):
         cfg = _abi.make_config(solver="EulerRoe", size=(n, n), boundary="PERIODIC", limiter="MinMod",
@@ -483,20 +484,26 @@ def adjoint_measure(hg, _abi, ic, args):
         f, bw = cp.times()
         fwd_ms += f
         bwd_ms += bw
-        # the same trajectory with every step's tape recorded during the forward
+        # the same trajectory with every step's tape recorded during the forward (its
+        # tapes must fit on the device: refused with HGPU_ERR_NOMEM otherwise)
         cp.close()
-        s_.resetState(u0)
-        ct = hg.Checkpoints(s_, args.adjoint_steps, taped=True)
-        ct.forward()
-        gt = torch.empty_like(dl)
-        torch.cuda.synchronize()
-        ct.backward(dl.data_ptr(), gt.data_ptr())
-        s_.synchronize()
-        f, bw = ct.times()
-        tfwd_ms += f
-        tbwd_ms += bw
-        taped_same = taped_same and np.array_equal(ct.dts(), dts) and bool(torch.equal(gt, g))
-        ct.close()
+        if taped_error is None:
+            s_.resetState(u0)
+            try:
+                ct = hg.Checkpoints(s_, args.adjoint_steps, taped=True)
+            except hg.HgpuError as e:
+                taped_error = str(e)
+            else:
+                ct.forward()
+                gt = torch.empty_like(dl)
+                torch.cuda.synchronize()
+                ct.backward(dl.data_ptr(), gt.data_ptr())
+                s_.synchronize()
+                f, bw = ct.times()
+                tfwd_ms += f
+                tbwd_ms += bw
+                taped_same = taped_same and np.array_equal(ct.dts(), dts) and bool(torch.equal(gt, g))
+                ct.close()
         if k == 0 and args.fd_directions > 0:
             gh = g.cpu().numpy()
             rng = np.random.default_rng(300)
@@ -526,7 +533,7 @@ def adjoint_measure(hg, _abi, ic, args):
         "forward_ms_per_step": fwd_ms / steps_total, "plain_forward_ms_per_step": plain_ms / steps_total,
         "backward_ms_per_step": bwd_ms / steps_total,
         "adjoint_over_forward": bwd_ms / fwd_ms, "adjoint_over_plain_forward": bwd_ms / plain_ms,
-        "taped": {
+        "taped": {"unavailable": taped_error} if taped_error else {
             "note": "every step's tape recorded during the forward (hgpu_checkpoint_create_taped): the "
                     "backward runs the reverse steps only",
             "forward_ms_per_step": tfwd_ms / steps_total, "backward_ms_per_step": tbwd_ms / steps_total,
@@ -585,7 +592,7 @@ def summary_block(value, e2e, roofline, batched, adjoint, fused=None):
         out["adjoint_over_forward"] = adjoint["adjoint_over_forward"]
         out["adjoint_over_plain_forward"] = adjoint["adjoint_over_plain_forward"]
         tp = adjoint.get("taped")
-        if tp:
+        if tp and "unavailable" not in tp:
             out["taped_adjoint_over_plain_forward"] = tp["adjoint_over_plain_forward"]
             out["taped_gradient_over_plain_forward"] = tp["gradient_over_plain_forward"]
         fd = adjoint.get("finite_differences")

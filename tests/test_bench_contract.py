@@ -79,3 +79,13 @@ def test_summary_block_keys(bench):
     assert out["batched_speedup_vs_plain_sequential"] == 3.3
     assert out["taped_adjoint_over_plain_forward"] == 1.85
     assert out["fd_within_1e-6"] == "0/64" and out["fd_differentiable_within_1e-6"] == "7/8"
+
+
+def test_summary_block_without_taped_adjoint(bench):
+    roof = {"frac": 0.78, "hbm": {"frac": 0.25}, "hbm_step": {"frac": 0.04}}
+    adjoint = {"adjoint_over_forward": 2.93, "adjoint_over_plain_forward": 2.96,
+               "taped": {"unavailable": "the tapes of every step do not fit in device memory"}}
+    out = bench.summary_block(5.4e8, None, roof, None, adjoint)
+    assert out["adjoint_over_plain_forward"] == 2.96
+    assert "taped_adjoint_over_plain_forward" not in out
+    assert out["e2e"] is None
